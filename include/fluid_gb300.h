@@ -1,0 +1,213 @@
+/*
+ * fluid_gb300.h -- C ABI of libfluidgb, a GB300 (sm_103a) implementation of the
+ * Position Based Fluids step and the marching-cubes surface extraction of libfluid.
+ *
+ * Every entry point returns an int status (FGB_OK == 0); the message of the last
+ * failure on the calling thread is returned by fgb_last_error().  No C++ or torch
+ * type crosses this boundary: plain pointers, sizes and POD structs only.
+ *
+ * Reference interface being replaced (tom91136/libfluid):
+ *   include/fluid/fluid.hpp:222-232   fluid::SphSolver<T,N>::advance (pure virtual)
+ *   include/fluid/oclsph.hpp:170-189  ocl::SphSolver(h, kernelPath, device)
+ *   include/fluid/oclsph.hpp:661-936  ocl::SphSolver::advance (predict, grid, solve, MC)
+ *   include/fluid/oclsph_type.h:6-56  ClSphConfig / ClMcConfig / ClSphTraiangle PODs
+ */
+#ifndef FLUID_GB300_H
+#define FLUID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FGB_VERSION 1
+
+/* status codes */
+#define FGB_OK              0
+#define FGB_ERR_INVALID     1  /* bad argument or configuration */
+#define FGB_ERR_CUDA        2  /* a CUDA runtime call failed */
+#define FGB_ERR_OOM         3  /* device or host allocation failed */
+#define FGB_ERR_CAPACITY    4  /* a size is beyond a documented maximum */
+#define FGB_ERR_TIMEOUT     5  /* a bounded device-side wait gave up (error flag set) */
+#define FGB_ERR_UNSUPPORTED 6
+#define FGB_ERR_BUDGET      7  /* serving: request larger than the HBM budget */
+
+/* physics profiles */
+#define FGB_PROFILE_REF      0 /* reference constants and formulas (oclsph_kernel.h:20-35) */
+#define FGB_PROFILE_BASELINE 1 /* textbook PBF with s_corr, XSPH and vorticity confinement */
+
+/* particle types (fluid.hpp:18-20) */
+#define FGB_TYPE_FLUID    0
+#define FGB_TYPE_OBSTACLE 1
+
+#define FGB_MAX_WELLS 16
+
+/* Solver constants, fixed per solver like the reference's -DSPH_H build flag
+ * (oclsph.hpp:178) and its compile-time constants (oclsph_kernel.h:20-35). */
+typedef struct fgb_params {
+    float h;                     /* smoothing length == grid cell size (solver units) */
+    int32_t profile;             /* FGB_PROFILE_* */
+    float rho0;                  /* rest density (ref 6378, baseline 1000) */
+    float cfm_epsilon;           /* lambda relaxation (ref 600, baseline 100) */
+    float corr_k;                /* s_corr k (ref 1e-4, baseline 0.1) */
+    float corr_n;                /* s_corr exponent n (4) */
+    float corr_delta_q;          /* s_corr delta q as a fraction of h (ref 0.3, baseline 0.2) */
+    float xsph_c;                /* XSPH viscosity c (baseline 0.01; unused by ref) */
+    float vorticity_epsilon;     /* vorticity confinement epsilon (baseline 5e-4; unused by ref) */
+    float velocity_damping;      /* ref finalise factor VD (0.49); unused by baseline */
+    float mc_particle_size;      /* ref metaball size (oclsph.hpp:672, 25) */
+    float mc_particle_influence; /* ref metaball exponent (oclsph.hpp:673, 0.5) */
+} fgb_params;
+
+/* A well pulls fluid particles within 75 world units (oclsph.hpp:306-317; fluid.hpp:137-144). */
+typedef struct fgb_well {
+    float centre[3];
+    float force;
+} fgb_well;
+
+/* Per-call configuration; mirrors fluid::Config (fluid.hpp:172-209) minus the
+ * host-side vectors (sources, drains and queries stay in the C++ adapter). */
+typedef struct fgb_config {
+    float dt;
+    float scale;
+    float resolution;            /* MC samples per h (sampleResolution, oclsph.hpp:671) */
+    float isolevel;
+    uint32_t iterations;         /* solver iterations per step */
+    uint32_t surface;            /* 1: fgb_advance also runs marching cubes */
+    float constant_force[3];
+    float min_bound[3];
+    float max_bound[3];
+    int32_t sphere_enabled;      /* analytic static sphere collider (world units) */
+    float sphere[4];             /* centre xyz, radius */
+    uint32_t n_wells;
+    fgb_well wells[FGB_MAX_WELLS];
+} fgb_config;
+
+/* Host particle view, structure of arrays (the adapter copies fluid::Particle
+ * field by field, so the ABI never depends on a GLM vector layout). */
+typedef struct fgb_particles {
+    size_t n;
+    uint64_t *id;
+    int32_t *type;
+    float *mass;
+    float *position;   /* 3n, xyz interleaved */
+    float *velocity;   /* 3n */
+    uint32_t *colour;  /* ARGB */
+} fgb_particles;
+
+/* Collider triangle (ClSphTraiangle, oclsph_type.h:47-51). */
+typedef struct fgb_triangle {
+    float a[3], b[3], c[3];
+} fgb_triangle;
+
+/* Surface triangle; same field order as geometry::MeshTriangle<float> (geometry.hpp:40-44). */
+typedef struct fgb_mesh_triangle {
+    float v[9];        /* v0, v1, v2 */
+    float n[9];        /* n0, n1, n2 */
+    uint32_t c[3];     /* per-vertex ARGB colour */
+} fgb_mesh_triangle;
+
+typedef struct fgb_mesh {
+    fgb_mesh_triangle *triangles; /* owned by the library; release with fgb_mesh_free */
+    size_t n;
+    size_t capacity;
+} fgb_mesh;
+
+typedef struct fgb_solver fgb_solver;
+typedef struct fgb_batch fgb_batch;
+typedef struct fgb_server fgb_server;
+
+/* ---- library ---------------------------------------------------------- */
+int fgb_version(void);
+/* Message of the last failure on this thread ("" when none). */
+const char *fgb_last_error(void);
+/* Fills constants of a profile; the ref profile replaces oclsph_kernel.h:20-35. */
+void fgb_params_default(fgb_params *p, int32_t profile, float h);
+/* Fills a config with the reference demo's defaults (samples/main.cpp:398-411) or,
+ * for the baseline profile, the dam-break workload parameters. */
+void fgb_config_default(fgb_config *c, int32_t profile);
+
+/* ---- solver: replaces ocl::SphSolver (oclsph.hpp:150-189) --------------- */
+int fgb_create(const fgb_params *params, fgb_solver **out);
+int fgb_destroy(fgb_solver *s);
+/* Launch all work of this solver on a caller-owned cudaStream_t (NULL: the
+ * library's own stream). */
+int fgb_set_stream(fgb_solver *s, void *cuda_stream);
+/* One frame, with the reference's contract (oclsph.hpp:661-936): xs is read,
+ * advanced and written back REORDERED into Morton order; obstacles keep their
+ * state; if cfg->surface, marching cubes runs and mesh_out receives triangles
+ * (mesh_out may be NULL).  Host buffers in, host buffers out. */
+int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs,
+                const fgb_triangle *colliders, size_t n_colliders, fgb_mesh *mesh_out);
+void fgb_mesh_free(fgb_mesh *m);
+
+/* ---- resident scenes (a batch of one is the single-scene path) ---------- */
+/* Scenes keep particles, grid and sort scratch on the device between steps.
+ * All scenes of a batch share the solver constants and the iteration count. */
+int fgb_batch_create(fgb_solver *s, uint32_t n_scenes, const uint64_t *counts,
+                     const fgb_config *configs, fgb_batch **out);
+int fgb_batch_destroy(fgb_batch *b);
+int fgb_batch_upload(fgb_batch *b, uint32_t scene, const fgb_particles *xs);
+int fgb_batch_set_colliders(fgb_batch *b, uint32_t scene, const fgb_triangle *tris, size_t n);
+/* Advance every scene of the batch by `steps` steps: one launch per stage for
+ * all scenes, replayed from a CUDA graph. Asynchronous on the solver stream. */
+int fgb_batch_step(fgb_batch *b, uint32_t steps);
+int fgb_batch_download(fgb_batch *b, uint32_t scene, fgb_particles *xs);
+/* Marching cubes of one scene's current state; synchronous. */
+int fgb_batch_surface(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
+/* Marching cubes of every scene in one launch per stage; triangle counts only
+ * (counts[n_scenes]); triangles of scene k via fgb_batch_surface_fetch. */
+int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts);
+int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
+int fgb_batch_sync(fgb_batch *b);
+/* Device error flags raised by bounded waits since the last call (0: none). */
+int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags);
+/* Number of kernels this batch launched since creation (for accounting). */
+uint64_t fgb_batch_launch_count(const fgb_batch *b);
+
+/* Parity probes: copy an internal array of the last step to host memory.
+ * what: FGB_PROBE_* ; bytes must equal the array size. */
+#define FGB_PROBE_KEYS        1 /* u32 sorted keys (scene << morton_bits | morton) */
+#define FGB_PROBE_ORDER       2 /* u32 slot of each sorted particle (its index at upload) */
+#define FGB_PROBE_CELLS       3 /* u32 pairs {start,end} per Morton key, all scenes' tables */
+#define FGB_PROBE_LAMBDA      4 /* f32 lambda of the last solver iteration */
+#define FGB_PROBE_DENSITY     5 /* f32 density of the last solver iteration */
+#define FGB_PROBE_LATTICE     6 /* f32x4 MC lattice (value, normal) of the last surface call */
+#define FGB_PROBE_CUBE_CASES  7 /* u8 MC case index per cube of the last surface call */
+int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes);
+int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes);
+/* Grid geometry of a scene: minimum extent (solver units), cell extent,
+ * table offset/size and Morton bits of the batch. */
+typedef struct fgb_grid_info {
+    float min_extent[3];
+    uint32_t extent[3];
+    uint64_t table_offset;
+    uint64_t table_size;
+    uint32_t morton_bits;
+    uint32_t scene_bits;
+    uint32_t lattice[3];      /* MC lattice samples per axis */
+    float lattice_origin[3];  /* solver units */
+    float lattice_step;       /* solver units */
+} fgb_grid_info;
+int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out);
+
+/* ---- device building blocks (device pointers, caller-provided scratch) --- */
+/* Stable LSD radix sort of (key, value) u32 pairs on the low key_bits bits. */
+uint64_t fgb_radix_sort_scratch_bytes(uint64_t n);
+int fgb_radix_sort_pairs_u32(const uint32_t *d_keys_in, const uint32_t *d_vals_in,
+                             uint32_t *d_keys_out, uint32_t *d_vals_out, uint64_t n,
+                             uint32_t key_bits, void *d_scratch, uint64_t scratch_bytes,
+                             void *cuda_stream);
+/* Single-pass exclusive prefix sum of u32 (decoupled look-back); writes the
+ * total to d_total (device) when not NULL. */
+uint64_t fgb_scan_scratch_bytes(uint64_t n);
+int fgb_exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
+                           void *d_scratch, uint64_t scratch_bytes, void *cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUID_GB300_H */

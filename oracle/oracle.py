@@ -1,0 +1,195 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module, as the checker or the timed CPU baseline; the product never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_shim.so")
+
+_lib = None
+_ref = None
+
+
+def build(quiet=True):
+    """Compile the oracle (and the reference shim where the reference tree exists)."""
+    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if not quiet:
+        print(out.stdout)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        from libfluid_gb300 import capi
+        L = ctypes.CDLL(LIB)
+        P = ctypes.POINTER
+        vp = ctypes.c_void_p
+        L.orc_morton.restype = ctypes.c_uint32
+        L.orc_morton.argtypes = [ctypes.c_uint32] * 3
+        L.orc_morton_decode.restype = ctypes.c_uint32
+        L.orc_morton_decode.argtypes = [ctypes.c_uint32, ctypes.c_int]
+        L.orc_mc_tables.argtypes = [vp, vp, vp]
+        L.orc_poly6.restype = ctypes.c_float
+        L.orc_poly6.argtypes = [P(capi.Params), ctypes.c_float]
+        L.orc_spiky_scale.restype = ctypes.c_float
+        L.orc_spiky_scale.argtypes = [P(capi.Params), ctypes.c_float]
+        L.orc_grid_geometry.argtypes = [P(capi.Params), P(capi.Config), vp]
+        L.orc_lattice_geometry.argtypes = [P(capi.Params), P(capi.Config), vp, vp]
+        L.orc_step.restype = ctypes.c_int
+        L.orc_step.argtypes = [P(capi.Params), P(capi.Config), ctypes.c_size_t, vp, vp, vp, vp, vp, vp,
+                               vp, ctypes.c_size_t, vp]
+        L.orc_surface.restype = ctypes.c_size_t
+        L.orc_surface.argtypes = [P(capi.Params), P(capi.Config), ctypes.c_size_t, vp, vp, vp, vp, vp,
+                                  vp, vp, vp, ctypes.c_size_t]
+        L.orc_march.restype = ctypes.c_size_t
+        L.orc_march.argtypes = [P(capi.Params), P(capi.Config), vp, vp, vp, vp, vp, ctypes.c_size_t]
+        L.orc_num_threads.restype = ctypes.c_int
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own curves.h / mctable.hpp / mc.h, or None when not built."""
+    global _ref
+    if _ref is None and os.path.exists(REF_LIB):
+        R = ctypes.CDLL(REF_LIB)
+        R.ref_morton.restype = ctypes.c_uint64
+        R.ref_morton.argtypes = [ctypes.c_uint64] * 3
+        R.ref_morton_decode.restype = ctypes.c_uint64
+        R.ref_morton_decode.argtypes = [ctypes.c_uint64, ctypes.c_int]
+        for f in ("ref_edge_table", "ref_num_verts", "ref_cl_edge_table", "ref_cl_num_verts"):
+            getattr(R, f).restype = ctypes.c_int
+            getattr(R, f).argtypes = [ctypes.c_int]
+        for f in ("ref_tri_table", "ref_cl_tri_table"):
+            getattr(R, f).restype = ctypes.c_int
+            getattr(R, f).argtypes = [ctypes.c_int, ctypes.c_int]
+        _ref = R
+    return _ref
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("min_ext", ctypes.c_float * 3), ("ext", ctypes.c_uint32 * 3), ("table_n", ctypes.c_uint32)]
+
+
+class Lattice(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32 * 3), ("origin", ctypes.c_float * 3), ("step", ctypes.c_float)]
+
+
+class Probe(ctypes.Structure):
+    _fields_ = [("keys", ctypes.c_void_p), ("order", ctypes.c_void_p), ("cells", ctypes.c_void_p),
+                ("lambda_", ctypes.c_void_p), ("density", ctypes.c_void_p)]
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def mc_tables():
+    em = np.zeros(256, np.uint16)
+    nv = np.zeros(256, np.uint8)
+    tri = np.zeros((256, 16), np.uint8)
+    lib().orc_mc_tables(_ptr(em), _ptr(nv), _ptr(tri))
+    return em, nv, tri
+
+
+def grid(params, cfg):
+    g = Grid()
+    lib().orc_grid_geometry(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(g))
+    return g
+
+
+def lattice(params, cfg):
+    g = grid(params, cfg)
+    l = Lattice()
+    lib().orc_lattice_geometry(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(g), ctypes.byref(l))
+    return l
+
+
+def step(params, cfg, parts, colliders=None, probe=False):
+    """One step in place on a dict of arrays (see libfluid_gb300.scenes.block).
+    Returns the probe dict when probe=True."""
+    n = len(parts["mass"])
+    pr = None
+    out = None
+    if probe:
+        g = grid(params, cfg)
+        out = {
+            "keys": np.zeros(n, np.uint32),
+            "order": np.zeros(n, np.uint32),
+            "cells": np.zeros(2 * g.table_n, np.uint32),
+            "lambda": np.zeros(n, np.float32),
+            "density": np.zeros(n, np.float32),
+        }
+        pr = Probe(_ptr(out["keys"]), _ptr(out["order"]), _ptr(out["cells"]), _ptr(out["lambda"]),
+                   _ptr(out["density"]))
+    tris = None
+    ntris = 0
+    if colliders is not None and len(colliders):
+        tris = np.ascontiguousarray(colliders, np.float32)
+        ntris = len(tris)
+    rc = lib().orc_step(ctypes.byref(params), ctypes.byref(cfg), n, _ptr(parts["id"]), _ptr(parts["type"]),
+                        _ptr(parts["mass"]), _ptr(parts["position"]), _ptr(parts["velocity"]),
+                        _ptr(parts["colour"]), _ptr(tris) if tris is not None else None, ntris,
+                        ctypes.byref(pr) if pr is not None else None)
+    if rc != 0:
+        raise RuntimeError("oracle step failed")
+    return out
+
+
+def surface(params, cfg, parts, want_lattice=False):
+    """Marching cubes of the current state: (triangles[n,21], lattice, colours, cases)."""
+    n = len(parts["mass"])
+    l = lattice(params, cfg)
+    samples = l.size[0] * l.size[1] * l.size[2]
+    cubes = max(l.size[0] - 1, 0) * max(l.size[1] - 1, 0) * max(l.size[2] - 1, 0)
+    lat = np.zeros(4 * samples, np.float32)
+    lcol = np.zeros(samples, np.uint32)
+    cases = np.zeros(max(cubes, 1), np.uint8)
+    L = lib()
+    total = L.orc_surface(ctypes.byref(params), ctypes.byref(cfg), n, _ptr(parts["type"]), _ptr(parts["mass"]),
+                          _ptr(parts["position"]), _ptr(parts["colour"]), _ptr(lat), _ptr(lcol),
+                          _ptr(cases), None, 0)
+    tris = np.zeros((max(total, 1), 21), np.float32)
+    total2 = L.orc_march(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(l), _ptr(lat), _ptr(lcol),
+                         None, _ptr(tris), total)
+    assert total2 == total
+    tris = tris[:total]
+    if want_lattice:
+        return tris, lat.reshape(-1, 4), lcol, cases[:cubes]
+    return tris
+
+
+def march(params, cfg, lat, lcol):
+    """Marching cubes of a given lattice (stage-wise parity)."""
+    l = lattice(params, cfg)
+    cubes = (l.size[0] - 1) * (l.size[1] - 1) * (l.size[2] - 1)
+    cases = np.zeros(max(cubes, 1), np.uint8)
+    lat = np.ascontiguousarray(lat, np.float32)
+    lcol = np.ascontiguousarray(lcol, np.uint32)
+    L = lib()
+    total = L.orc_march(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(l), _ptr(lat), _ptr(lcol),
+                        _ptr(cases), None, 0)
+    tris = np.zeros((max(total, 1), 21), np.float32)
+    L.orc_march(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(l), _ptr(lat), _ptr(lcol), None,
+                _ptr(tris), total)
+    return tris[:total], cases[:cubes]
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def num_threads():
+    return int(lib().orc_num_threads())
