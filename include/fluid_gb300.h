@@ -123,6 +123,11 @@ typedef struct fgb_server fgb_server;
 int fgb_version(void);
 /* Message of the last failure on this thread ("" when none). */
 const char *fgb_last_error(void);
+/* sizeof of the ABI structs in this order: fgb_params, fgb_config, fgb_particles,
+ * fgb_triangle, fgb_mesh_triangle, fgb_mesh, fgb_grid_info, fgb_well; writes at most
+ * n values and returns how many exist.  Replaces the reference's check_size kernel
+ * and host assert of struct layouts (oclsph_kernel.h:276-278, oclsph.hpp:217-243). */
+int fgb_struct_sizes(uint64_t *out, int n);
 /* Fills constants of a profile; the ref profile replaces oclsph_kernel.h:20-35. */
 void fgb_params_default(fgb_params *p, int32_t profile, float h);
 /* Fills a config with the reference demo's defaults (samples/main.cpp:398-411) or,

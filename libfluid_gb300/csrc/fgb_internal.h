@@ -1,0 +1,94 @@
+// fgb_internal.h -- host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fluid_gb300.h"
+#include "fgb_device.cuh"
+
+namespace fgb {
+
+// Thread-local last-error message behind fgb_last_error(); both return `code`.
+int fail(int code, const char *msg);
+int fail_cuda(cudaError_t e, const char *where);
+
+// radix sort (sort.cu)
+uint64_t radix_scratch_bytes(uint64_t n);
+int radix_passes(uint32_t key_bits);
+cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                             uint32_t *vals_out, uint64_t n, uint32_t key_bits, void *scratch,
+                             uint64_t scratch_bytes, cudaStream_t stream, uint32_t *err, uint64_t *launches);
+
+// prefix scan of a u32 array (scan.cu)
+uint64_t scan_u32_scratch_bytes(uint64_t n);
+cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint32_t *total, uint64_t n, void *scratch,
+                     uint64_t scratch_bytes, cudaStream_t stream, uint32_t *err, uint64_t *launches);
+
+// PBF stages (pbf.cu).  Arrays are indexed by particle over the whole batch.
+struct StepView {
+    const SceneDev *scenes;
+    const WellDev *wells;
+    const TriDev *tris;
+    uint32_t n;
+    uint32_t mbits;
+    Phys ph;
+    // state at step start (current order)
+    const float4 *x0, *v0;
+    const int32_t *type0;
+    const uint32_t *col0, *slot0;
+    // state in sorted order
+    float4 *x1, *v1;
+    int32_t *type1;
+    uint32_t *col1, *slot1;
+    // step temporaries
+    uint32_t *keys_prev;   // sorted keys of the previous step (scene id in the high bits)
+    uint32_t *keys_in, *vals_in, *keys_sorted, *vals_sorted;
+    uint2 *cells;
+    uint64_t cells_n;
+    float4 *ps_a, *ps_b;
+    float *lambda, *density;
+    float4 *omega, *vx;
+    uint32_t *err;
+    int block;             // threads per CTA of the gather kernels
+};
+
+void launch_predict_keys(const StepView &s, cudaStream_t st);
+void launch_reorder_cells(const StepView &s, cudaStream_t st);
+void launch_lambda(const StepView &s, const float4 *ps, cudaStream_t st);
+void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool last, cudaStream_t st);
+void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st);
+// keys of the current positions (marching-cubes grid); ps_a receives solver-unit
+// positions in sorted order, cells the table
+void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st);
+void launch_gather_positions(const StepView &s, const float4 *x, const int32_t *type, const uint32_t *col,
+                             float4 *xs_sorted, int32_t *type_sorted, uint32_t *col_sorted, cudaStream_t st);
+
+// marching cubes (mc.cu)
+struct SurfaceView {
+    const SceneDev *scenes;   // device
+    const SceneDev *h_scenes; // host copy
+    uint32_t scene_begin, scene_end;
+    uint32_t mbits;
+    Phys ph;
+    const uint32_t *keys_sorted;
+    const uint2 *cells;
+    const float4 *xs;        // sorted, solver units, w = mass
+    const int32_t *type;
+    const uint32_t *col;
+    float4 *lattice;
+    uint32_t *lattice_col;
+    uint8_t *cases;
+    uint32_t *offsets;
+    uint32_t *total;         // device, one u32
+    uint64_t lat_begin, lat_end, cube_begin, cube_end;
+    void *scan_scratch;
+    uint64_t scan_scratch_bytes;
+    uint32_t *err;
+};
+cudaError_t launch_surface_count(const SurfaceView &v, cudaStream_t st, uint64_t *launches);
+cudaError_t launch_surface_emit(const SurfaceView &v, fgb_mesh_triangle *out, uint64_t cap, cudaStream_t st,
+                                uint64_t *launches);
+void mc_tables_upload();
+
+}  // namespace fgb

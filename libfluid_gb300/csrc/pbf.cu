@@ -1,0 +1,563 @@
+// pbf.cu -- the Position Based Fluids step as sm_103a gather kernels.
+//
+// One step (all scenes of a batch in one launch per stage):
+//   k_predict_keys   predict p* and its 30-bit Morton key  (oclsph.hpp:289-387)
+//   radix sort       (sort.cu)                              (oclsph.hpp:733-743)
+//   k_reorder_cells  gather the state into sorted SoA float4 and write each cell's
+//                    {start, end} by adjacent difference    (oclsph.hpp:746-767, 822-853)
+//   iterations x {k_lambda, k_delta}                        (oclsph_kernel.h:305-384)
+//   k_delta(last)    also finalises x / v                   (oclsph_kernel.h:404-416)
+//   baseline only:   k_vorticity_xsph, k_vorticity_apply    (PBF paper eq. 15-17)
+// Gathers walk the 27 neighbour cells in the reference's order (dz, dy, dx with x
+// fastest, oclsph_kernel.h:155-183) and each cell's particles in sorted order, so
+// every per-particle sum has one fixed order.  The solve is Jacobi: k_delta reads
+// one p* buffer and writes the other (the reference updates p* in place, a race).
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fgb_internal.h"
+
+namespace fgb {
+namespace {
+
+constexpr int kRef = FGB_PROFILE_REF;
+
+// Predicted position of one particle in solver units (oclsph.hpp:297-323).
+__device__ __forceinline__ float3 predict(const Phys &ph, const SceneDev &S, const WellDev *wells, int32_t type,
+                                          float4 x, float4 v) {
+    float3 ps = make_float3(x.x / S.scale, x.y / S.scale, x.z / S.scale);
+    if (type == FGB_TYPE_OBSTACLE) return ps;
+    const bool ref = ph.profile == kRef;
+    const float mass = x.w;
+    float f[3];
+    for (int a = 0; a < 3; ++a) f[a] = ref ? mass * S.g[a] : S.g[a];
+    const float xa[3] = {x.x, x.y, x.z};
+    for (uint32_t w = 0; w < S.n_wells; ++w) {
+        const WellDev wl = wells[S.well_first + w];
+        float d0 = xa[0] - wl.centre[0], d1 = xa[1] - wl.centre[1], d2 = xa[2] - wl.centre[2];
+        float dist = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+        if (dist < 75.f) {
+            float u0 = wl.centre[0] - xa[0], u1 = wl.centre[1] - xa[1], u2 = wl.centre[2] - xa[2];
+            float ul = sqrtf(u0 * u0 + u1 * u1 + u2 * u2);
+            const float u[3] = {u0, u1, u2};
+            for (int a = 0; a < 3; ++a) {
+                float rhat = u[a] / ul;
+                float fw = ref ? ((rhat * wl.force) * mass) / (dist * dist) : (rhat * wl.force) / (dist * dist);
+                if (fw < -10.f) fw = -10.f;
+                if (fw > 10.f) fw = 10.f;
+                f[a] = f[a] + fw;
+            }
+        }
+    }
+    const float va[3] = {v.x, v.y, v.z};
+    float p[3];
+    for (int a = 0; a < 3; ++a) {
+        float vn = f[a] * S.dt + va[a];
+        p[a] = vn * S.dt + xa[a] / S.scale;
+    }
+    return make_float3(p[0], p[1], p[2]);
+}
+
+__device__ __forceinline__ uint32_t cell_key(const SceneDev &S, float h, float x, float y, float z) {
+    return morton3(quantise(x, S.min_ext[0], h, S.ext[0]), quantise(y, S.min_ext[1], h, S.ext[1]),
+                   quantise(z, S.min_ext[2], h, S.ext[2]));
+}
+
+template <class F>
+__device__ __forceinline__ void for_neighbours(const SceneDev &S, const uint2 *__restrict__ cells, uint32_t key,
+                                               uint32_t mbits, F &&f) {
+    const uint32_t m = morton_of(key, mbits);
+    for_neighbour_cells(S, cells, (int)compact10(m), (int)compact10(m >> 1), (int)compact10(m >> 2), f);
+}
+
+__global__ void k_predict_keys(const SceneDev *__restrict__ scenes, const WellDev *__restrict__ wells, Phys ph,
+                               uint32_t n, uint32_t mbits, const uint32_t *__restrict__ keys_prev,
+                               const float4 *__restrict__ x, const float4 *__restrict__ v,
+                               const int32_t *__restrict__ type, uint32_t *__restrict__ keys_out,
+                               uint32_t *__restrict__ vals_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t s = scene_of(keys_prev[i], mbits);
+        const SceneDev &S = scenes[s];
+        const float3 p = predict(ph, S, wells, type[i], x[i], v[i]);
+        const uint32_t m = cell_key(S, ph.h, p.x, p.y, p.z);
+        keys_out[i] = (mbits >= 32 ? 0u : (s << mbits)) | m;
+        vals_out[i] = i;
+    }
+}
+
+// Gather the state into sorted order, recompute p* there (same bits as
+// k_predict_keys), and write each occupied cell's {start, end}.
+__global__ void k_reorder_cells(const SceneDev *__restrict__ scenes, const WellDev *__restrict__ wells, Phys ph,
+                                uint32_t n, uint32_t mbits, const uint32_t *__restrict__ keys,
+                                const uint32_t *__restrict__ vals, const float4 *__restrict__ x0,
+                                const float4 *__restrict__ v0, const int32_t *__restrict__ type0,
+                                const uint32_t *__restrict__ col0, const uint32_t *__restrict__ slot0,
+                                float4 *__restrict__ x1, float4 *__restrict__ v1, int32_t *__restrict__ type1,
+                                uint32_t *__restrict__ col1, uint32_t *__restrict__ slot1,
+                                float4 *__restrict__ ps, uint2 *__restrict__ cells, uint64_t cells_n,
+                                uint32_t *err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t j = vals[i];
+        const uint32_t key = keys[i];
+        const uint32_t s = scene_of(key, mbits);
+        const SceneDev &S = scenes[s];
+        const float4 xj = x0[j], vj = v0[j];
+        const int32_t tj = type0[j];
+        const float3 p = predict(ph, S, wells, tj, xj, vj);
+        x1[i] = xj;
+        v1[i] = vj;
+        type1[i] = tj;
+        col1[i] = col0[j];
+        slot1[i] = slot0[j];
+        ps[i] = make_float4(p.x, p.y, p.z, xj.w);
+        const uint64_t c = (uint64_t)S.table_base + morton_of(key, mbits);
+        if (c >= cells_n) {
+            raise_error(err, ERR_CELL_RANGE);
+            continue;
+        }
+        if (i == 0 || keys[i - 1] != key) cells[c].x = i;
+        if (i + 1 == n || keys[i + 1] != key) cells[c].y = i + 1;
+    }
+}
+
+template <int PROFILE>
+__global__ void __launch_bounds__(256) k_lambda(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n,
+                                                uint32_t mbits, const uint32_t *__restrict__ keys,
+                                                const uint2 *__restrict__ cells, const float4 *__restrict__ ps,
+                                                const int32_t *__restrict__ type, float *__restrict__ lambda,
+                                                float *__restrict__ density) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (type[a] == FGB_TYPE_OBSTACLE) {
+        lambda[a] = 0.f;
+        density[a] = 0.f;
+        return;
+    }
+    const uint32_t key = keys[a];
+    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const float4 pa = ps[a];
+    float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
+    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
+        const float4 pb = __ldg(&ps[b]);
+        const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (PROFILE == kRef) {
+            const float r = sqrtf(r2);
+            if (r <= ph.h) {
+                const float t = ph.hh - r * r;
+                rho = __fmaf_rn(pa.w, ph.poly6f * (t * t * t), rho);
+                if (r >= kKernelEpsilon) {
+                    const float hr = ph.h - r;
+                    const float sc = ph.spikyf * ((hr * hr) / r);
+                    gx = __fmaf_rn(dx * sc, ph.inv_rho0, gx);
+                    gy = __fmaf_rn(dy * sc, ph.inv_rho0, gy);
+                    gz = __fmaf_rn(dz * sc, ph.inv_rho0, gz);
+                }
+            }
+        } else {
+            if (r2 <= ph.hh) {
+                const float t = ph.hh - r2;
+                rho = __fmaf_rn(pb.w, t * t * t, rho);
+                const float r = sqrtf(r2);
+                if (r >= kKernelEpsilon) {
+                    const float hr = ph.h - r;
+                    const float sc = pb.w * ((hr * hr) / r);
+                    gx = __fmaf_rn(sc, dx, gx);
+                    gy = __fmaf_rn(sc, dy, gy);
+                    gz = __fmaf_rn(sc, dz, gz);
+                    g2 = __fmaf_rn(sc * sc, r2, g2);
+                }
+            }
+        }
+    });
+    float dens, lam;
+    if (PROFILE == kRef) {
+        dens = rho;
+        const float norm2 = gx * gx + gy * gy + gz * gz;
+        const float C = dens / ph.rho0 - 1.f;
+        lam = -C / (norm2 + ph.cfm);
+    } else {
+        dens = rho * ph.poly6f;
+        const float gs = ph.spikyf * ph.inv_rho0;
+        const float sx = gx * gs, sy = gy * gs, sz = gz * gs;
+        const float denom = (sx * sx + sy * sy + sz * sz) + g2 * (gs * gs);
+        const float C = dens * ph.inv_rho0 - 1.f;
+        lam = -C / (denom + ph.cfm);
+    }
+    lambda[a] = lam;
+    density[a] = dens;
+}
+
+__device__ __forceinline__ float corr_pow(float ratio, float n) {
+    if (n == 4.f) {
+        const float r2 = ratio * ratio;
+        return r2 * r2;
+    }
+    return powf(ratio, n);
+}
+
+__device__ __forceinline__ float dot3(const float *a, const float *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// oclsph_collision.h:7-58 (first containing triangle within 40 world units wins).
+__device__ void collide_triangles(const TriDev *__restrict__ tris, uint32_t first, uint32_t count, float *pos,
+                                  float *vel) {
+    for (uint32_t i = 0; i < count; ++i) {
+        const TriDev t = tris[first + i];
+        float e1[3], e2[3], nrm[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = t.b[a] - t.a[a];
+            e2[a] = t.c[a] - t.a[a];
+        }
+        nrm[0] = e1[1] * e2[2] - e1[2] * e2[1];
+        nrm[1] = e1[2] * e2[0] - e1[0] * e2[2];
+        nrm[2] = e1[0] * e2[1] - e1[1] * e2[0];
+        const float len = sqrtf(dot3(nrm, nrm));
+        const float nn[3] = {nrm[0] / len, nrm[1] / len, nrm[2] / len};
+        const float dist = dot3(nn, t.a) - dot3(nn, pos);
+        if (-40.f <= dist && dist <= 40.f) {
+            const float p0[3] = {pos[0] + nn[0] * dist, pos[1] + nn[1] * dist, pos[2] + nn[2] * dist};
+            float v0[3], v1[3], v2[3];
+            for (int a = 0; a < 3; ++a) {
+                v0[a] = t.c[a] - t.a[a];
+                v1[a] = t.b[a] - t.a[a];
+                v2[a] = p0[a] - t.a[a];
+            }
+            const float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d02 = dot3(v0, v2);
+            const float d11 = dot3(v1, v1), d12 = dot3(v1, v2);
+            const float inv = 1.f / (d00 * d11 - d01 * d01);
+            const float u = (d11 * d02 - d01 * d12) * inv;
+            const float w = (d00 * d12 - d01 * d02) * inv;
+            if ((u >= 0.f) && (w >= 0.f) && (u + w < 1.f)) {
+                const float vn = dot3(vel, nn);
+                for (int a = 0; a < 3; ++a) {
+                    vel[a] = vel[a] - (nn[a] * 2.f) * vn;
+                    pos[a] = p0[a];
+                }
+                return;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void collide_sphere(const SceneDev &S, float *pos) {
+    if (!S.sphere_enabled) return;
+    const float d[3] = {pos[0] - S.sphere[0], pos[1] - S.sphere[1], pos[2] - S.sphere[2]};
+    const float r = S.sphere[3];
+    const float d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    if (!(d2 < r * r)) return;
+    const float dist = sqrtf(d2);
+    if (dist > 0.f) {
+        const float s = r / dist;
+        for (int a = 0; a < 3; ++a) pos[a] = S.sphere[a] + d[a] * s;
+    } else {
+        pos[0] = S.sphere[0];
+        pos[1] = S.sphere[1] + r;
+        pos[2] = S.sphere[2];
+    }
+}
+
+template <int PROFILE>
+__global__ void __launch_bounds__(256)
+    k_delta(const SceneDev *__restrict__ scenes, const TriDev *__restrict__ tris, Phys ph, uint32_t n, uint32_t mbits,
+            const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells, const float4 *__restrict__ ps_in,
+            const float *__restrict__ lambda, const int32_t *__restrict__ type, float4 *__restrict__ ps_out,
+            float4 *__restrict__ x, float4 *__restrict__ v, int last) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const float4 pa = ps_in[a];
+    if (type[a] == FGB_TYPE_OBSTACLE) {
+        ps_out[a] = pa;
+        return;
+    }
+    const uint32_t key = keys[a];
+    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const float la = lambda[a];
+    float px = 0.f, py = 0.f, pz = 0.f;
+    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
+        const float4 pb = __ldg(&ps_in[b]);
+        const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (PROFILE == kRef) {
+            const float r = sqrtf(r2);
+            float w = 0.f;
+            if (r <= ph.h) {
+                const float t = ph.hh - r * r;
+                w = ph.poly6f * (t * t * t);
+            }
+            const float corr = -ph.corr_k * corr_pow(w / ph.corr_ref, ph.corr_n);
+            const float factor = (la + __ldg(&lambda[b]) + corr) / ph.rho0;
+            if (r >= kKernelEpsilon && r <= ph.h) {
+                const float hr = ph.h - r;
+                const float sc = ph.spikyf * ((hr * hr) / r);
+                px = __fmaf_rn(dx * sc, factor, px);
+                py = __fmaf_rn(dy * sc, factor, py);
+                pz = __fmaf_rn(dz * sc, factor, pz);
+            }
+        } else {
+            if (r2 <= ph.hh) {
+                const float r = sqrtf(r2);
+                if (r >= kKernelEpsilon) {
+                    const float t = ph.hh - r2;
+                    const float corr = -ph.corr_k * corr_pow((t * t * t) / ph.corr_wdq, ph.corr_n);
+                    const float hr = ph.h - r;
+                    const float sc = pb.w * ((hr * hr) / r) * (la + __ldg(&lambda[b]) + corr);
+                    px = __fmaf_rn(sc, dx, px);
+                    py = __fmaf_rn(sc, dy, py);
+                    pz = __fmaf_rn(sc, dz, pz);
+                }
+            }
+        }
+    });
+    float world[3];
+    if (PROFILE == kRef) {
+        world[0] = (pa.x + px) * S.scale;
+        world[1] = (pa.y + py) * S.scale;
+        world[2] = (pa.z + pz) * S.scale;
+    } else {
+        const float gs = ph.spikyf * ph.inv_rho0;
+        world[0] = (pa.x + px * gs) * S.scale;
+        world[1] = (pa.y + py * gs) * S.scale;
+        world[2] = (pa.z + pz * gs) * S.scale;
+        collide_sphere(S, world);
+    }
+    float4 va = v[a];
+    float vel[3] = {va.x, va.y, va.z};
+    if (S.tri_count) {
+        collide_triangles(tris, S.tri_first, S.tri_count, world, vel);
+        v[a] = make_float4(vel[0], vel[1], vel[2], va.w);
+    }
+    float q[3];
+    for (int d = 0; d < 3; ++d) {
+        float w = world[d];
+        w = fmaxf(S.min_b[d], w);
+        w = fminf(S.max_b[d], w);
+        q[d] = w / S.scale;
+    }
+    ps_out[a] = make_float4(q[0], q[1], q[2], pa.w);
+    if (last) {
+        const float4 xa = x[a];
+        const float xo[3] = {xa.x, xa.y, xa.z};
+        float nv[3], nx[3];
+        for (int d = 0; d < 3; ++d) {
+            const float dd = q[d] - xo[d] / S.scale;
+            if (PROFILE == kRef) {
+                nx[d] = q[d] * S.scale;
+                nv[d] = __fmaf_rn(dd, S.inv_dt, vel[d]) * ph.damping;
+            } else {
+                nv[d] = dd * S.inv_dt;
+            }
+        }
+        v[a] = make_float4(nv[0], nv[1], nv[2], va.w);
+        if (PROFILE == kRef) x[a] = make_float4(nx[0], nx[1], nx[2], xa.w);
+    }
+}
+
+__device__ __forceinline__ void cross3(const float *a, const float *b, float *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
+__global__ void __launch_bounds__(256)
+    k_vorticity_xsph(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
+                     const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
+                     const float4 *__restrict__ ps, const float4 *__restrict__ v, const int32_t *__restrict__ type,
+                     float4 *__restrict__ omega, float4 *__restrict__ vx) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const float4 va4 = v[a];
+    if (type[a] == FGB_TYPE_OBSTACLE) {
+        omega[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vx[a] = va4;
+        return;
+    }
+    const uint32_t key = keys[a];
+    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const float4 pa = ps[a];
+    const float va[3] = {va4.x, va4.y, va4.z};
+    float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
+    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
+        if (__ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
+        const float4 pb = __ldg(&ps[b]);
+        const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (!(r2 <= ph.hh)) return;
+        const float4 vb = __ldg(&v[b]);
+        const float vab[3] = {vb.x - va[0], vb.y - va[1], vb.z - va[2]};
+        const float t = ph.hh - r2;
+        const float mw = pb.w * (t * t * t);
+        xs[0] = __fmaf_rn(mw, vab[0], xs[0]);
+        xs[1] = __fmaf_rn(mw, vab[1], xs[1]);
+        xs[2] = __fmaf_rn(mw, vab[2], xs[2]);
+        const float r = sqrtf(r2);
+        if (r >= kKernelEpsilon) {
+            const float hr = ph.h - r;
+            const float sc = pb.w * ((hr * hr) / r);
+            float cr[3];
+            cross3(vab, d, cr);
+            o[0] = __fmaf_rn(sc, cr[0], o[0]);
+            o[1] = __fmaf_rn(sc, cr[1], o[1]);
+            o[2] = __fmaf_rn(sc, cr[2], o[2]);
+        }
+    });
+    const float gs = ph.spikyf * ph.inv_rho0;
+    const float ws = ph.poly6f * ph.inv_rho0;
+    const float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;
+    omega[a] = make_float4(ox, oy, oz, sqrtf(ox * ox + oy * oy + oz * oz));
+    vx[a] = make_float4(__fmaf_rn(ph.xsph_c, xs[0] * ws, va[0]), __fmaf_rn(ph.xsph_c, xs[1] * ws, va[1]),
+                        __fmaf_rn(ph.xsph_c, xs[2] * ws, va[2]), va4.w);
+}
+
+// Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
+__global__ void __launch_bounds__(256)
+    k_vorticity_apply(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
+                      const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
+                      const float4 *__restrict__ ps, const float4 *__restrict__ omega,
+                      const float4 *__restrict__ vx, const int32_t *__restrict__ type, float4 *__restrict__ v,
+                      float4 *__restrict__ x) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (type[a] == FGB_TYPE_OBSTACLE) return;
+    const uint32_t key = keys[a];
+    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const float4 pa = ps[a];
+    const float4 oa = omega[a];
+    float e[3] = {0.f, 0.f, 0.f};
+    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
+        if (__ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
+        const float4 pb = __ldg(&ps[b]);
+        const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        if (!(r2 <= ph.hh)) return;
+        const float r = sqrtf(r2);
+        if (!(r >= kKernelEpsilon)) return;
+        const float hr = ph.h - r;
+        const float sc = pb.w * ((hr * hr) / r) * (__ldg(&omega[b].w) - oa.w);
+        e[0] = __fmaf_rn(sc, d[0], e[0]);
+        e[1] = __fmaf_rn(sc, d[1], e[1]);
+        e[2] = __fmaf_rn(sc, d[2], e[2]);
+    });
+    const float gs = ph.spikyf * ph.inv_rho0;
+    const float ex = e[0] * gs, ey = e[1] * gs, ez = e[2] * gs;
+    const float el = sqrtf(ex * ex + ey * ey + ez * ez);
+    float N[3] = {0.f, 0.f, 0.f};
+    if (el > 0.f) {
+        N[0] = ex / el;
+        N[1] = ey / el;
+        N[2] = ez / el;
+    }
+    const float om[3] = {oa.x, oa.y, oa.z};
+    float f[3];
+    cross3(N, om, f);
+    const float4 vxa = vx[a];
+    const float ve = ph.vort_eps, dt = S.dt;
+    v[a] = make_float4(__fmaf_rn(dt, f[0] * ve, vxa.x), __fmaf_rn(dt, f[1] * ve, vxa.y),
+                       __fmaf_rn(dt, f[2] * ve, vxa.z), vxa.w);
+    const float4 xa = x[a];
+    x[a] = make_float4(pa.x * S.scale, pa.y * S.scale, pa.z * S.scale, xa.w);
+}
+
+// Keys of the current positions (marching-cubes grid).
+__global__ void k_position_keys(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
+                                const uint32_t *__restrict__ keys_prev, const float4 *__restrict__ x,
+                                uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t s = scene_of(keys_prev[i], mbits);
+        const SceneDev &S = scenes[s];
+        const float4 xi = x[i];
+        const uint32_t m = cell_key(S, ph.h, xi.x / S.scale, xi.y / S.scale, xi.z / S.scale);
+        keys_out[i] = (mbits >= 32 ? 0u : (s << mbits)) | m;
+        vals_out[i] = i;
+    }
+}
+
+__global__ void k_gather_positions(const SceneDev *__restrict__ scenes, uint32_t n, uint32_t mbits,
+                                   const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
+                                   const float4 *__restrict__ x, const int32_t *__restrict__ type,
+                                   const uint32_t *__restrict__ col, float4 *__restrict__ xs,
+                                   int32_t *__restrict__ type_s, uint32_t *__restrict__ col_s,
+                                   uint2 *__restrict__ cells, uint64_t cells_n, uint32_t *err) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t j = vals[i];
+        const uint32_t key = keys[i];
+        const SceneDev &S = scenes[scene_of(key, mbits)];
+        xs[i] = x[j];
+        type_s[i] = type[j];
+        col_s[i] = col[j];
+        const uint64_t c = (uint64_t)S.table_base + morton_of(key, mbits);
+        if (c >= cells_n) {
+            raise_error(err, ERR_CELL_RANGE);
+            continue;
+        }
+        if (i == 0 || keys[i - 1] != key) cells[c].x = i;
+        if (i + 1 == n || keys[i + 1] != key) cells[c].y = i + 1;
+    }
+}
+
+inline unsigned grid_for(uint32_t n, int block) {
+    unsigned g = (n + block - 1) / block;
+    return g ? g : 1;
+}
+
+inline unsigned stream_grid(uint32_t n) {
+    unsigned g = (n + 255) / 256;
+    const unsigned cap = 152u * 8u;
+    if (g > cap) g = cap;
+    return g ? g : 1;
+}
+
+}  // namespace
+
+void launch_predict_keys(const StepView &s, cudaStream_t st) {
+    k_predict_keys<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.wells, s.ph, s.n, s.mbits, s.keys_prev, s.x0, s.v0,
+                                                     s.type0, s.keys_in, s.vals_in);
+}
+
+void launch_reorder_cells(const StepView &s, cudaStream_t st) {
+    k_reorder_cells<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.wells, s.ph, s.n, s.mbits, s.keys_sorted,
+                                                      s.vals_sorted, s.x0, s.v0, s.type0, s.col0, s.slot0, s.x1,
+                                                      s.v1, s.type1, s.col1, s.slot1, s.ps_a, s.cells, s.cells_n,
+                                                      s.err);
+}
+
+void launch_lambda(const StepView &s, const float4 *ps, cudaStream_t st) {
+    if (s.ph.profile == FGB_PROFILE_REF)
+        k_lambda<FGB_PROFILE_REF><<<grid_for(s.n, s.block), s.block, 0, st>>>(
+            s.scenes, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps, s.type1, s.lambda, s.density);
+    else
+        k_lambda<FGB_PROFILE_BASELINE><<<grid_for(s.n, s.block), s.block, 0, st>>>(
+            s.scenes, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps, s.type1, s.lambda, s.density);
+}
+
+void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool last, cudaStream_t st) {
+    if (s.ph.profile == FGB_PROFILE_REF)
+        k_delta<FGB_PROFILE_REF><<<grid_for(s.n, s.block), s.block, 0, st>>>(
+            s.scenes, s.tris, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps_in, s.lambda, s.type1, ps_out, s.x1,
+            s.v1, last ? 1 : 0);
+    else
+        k_delta<FGB_PROFILE_BASELINE><<<grid_for(s.n, s.block), s.block, 0, st>>>(
+            s.scenes, s.tris, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps_in, s.lambda, s.type1, ps_out, s.x1,
+            s.v1, last ? 1 : 0);
+}
+
+void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st) {
+    k_vorticity_xsph<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
+                                                                  s.cells, ps, s.v1, s.type1, s.omega, s.vx);
+    k_vorticity_apply<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
+                                                                   s.cells, ps, s.omega, s.vx, s.type1, s.v1, s.x1);
+}
+
+void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st) {
+    k_position_keys<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_prev, x, s.keys_in,
+                                                      s.vals_in);
+}
+
+void launch_gather_positions(const StepView &s, const float4 *x, const int32_t *type, const uint32_t *col,
+                             float4 *xs_sorted, int32_t *type_sorted, uint32_t *col_sorted, cudaStream_t st) {
+    k_gather_positions<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.n, s.mbits, s.keys_sorted, s.vals_sorted, x,
+                                                         type, col, xs_sorted, type_sorted, col_sorted, s.cells,
+                                                         s.cells_n, s.err);
+}
+
+}  // namespace fgb

@@ -1,0 +1,1020 @@
+// runtime.cu -- host runtime behind the C ABI: solver, resident batches, surfaces.
+//
+// fgb_advance is the drop-in for ocl::SphSolver::advance (include/fluid/oclsph.hpp:
+// 661-936): it uploads the caller's particles, runs one step, writes them back in
+// Morton order and optionally extracts the surface.  Underneath, every scene lives in
+// a batch whose state stays in HBM between steps; a batch of one is the single-scene
+// path, so the drop-in, the batched workload and the serving loop share one code path.
+//
+// Device layout of a batch (n = particles of all scenes; scene k owns the contiguous
+// segment [first_k, first_k + count_k) of every array, kept by the sort because the
+// scene id sits above the Morton bits of the key):
+//   state (two sets, the step gathers one into the other in sorted order):
+//     x float4 (position xyz, mass), v float4, type i32, colour u32, slot u32
+//   step: keys/vals in + sorted (u32), radix scratch, cell table uint2 {start,end}
+//         per Morton key of every scene, p* float4 x2 (Jacobi ping-pong),
+//         lambda f32, density f32, omega float4, XSPH velocity float4
+//   surface (on first use): sorted positions, lattice float4 + colour u32 per
+//         sample, case u8 + offset u32 per cube, triangles
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fgb_internal.h"
+
+namespace fgb {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const char *msg) {
+    g_last_error = msg ? msg : "";
+    return code;
+}
+
+int fail_cuda(cudaError_t e, const char *where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    g_last_error = m;
+    if (e == cudaErrorMemoryAllocation) return FGB_ERR_OOM;
+    return FGB_ERR_CUDA;
+}
+
+#define FGB_CUDA(call, where)                         \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return fail_cuda(e_, where); \
+    } while (0)
+
+namespace {
+
+constexpr float kPi = 3.14159265358979323846f;
+
+template <class T>
+struct Dev {
+    T *p = nullptr;
+    size_t n = 0;
+    Dev() = default;
+    Dev(const Dev &) = delete;
+    Dev &operator=(const Dev &) = delete;
+    ~Dev() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        else p = nullptr;
+        return e;
+    }
+};
+
+template <class T>
+struct Pinned {
+    T *p = nullptr;
+    size_t n = 0;
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t ensure(size_t count) {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaHostAlloc((void **)&p, std::max<size_t>(count, 1) * sizeof(T), cudaHostAllocDefault);
+        if (e == cudaSuccess) n = std::max<size_t>(count, 1);
+        return e;
+    }
+};
+
+uint32_t bits_for(uint32_t v) {
+    uint32_t b = 0;
+    while ((1u << b) <= v && b < 31) ++b;
+    return b;
+}
+
+Phys make_phys(const fgb_params &p) {
+    Phys ph{};
+    const float h = p.h, hh = h * h, hhh = h * h * h;
+    ph.h = h;
+    ph.hh = hh;
+    ph.poly6f = 315.f / (64.f * kPi * (hhh * hhh * hhh));
+    ph.spikyf = -(45.f / (kPi * hhh * hhh));
+    ph.rho0 = p.rho0;
+    ph.inv_rho0 = 1.f / p.rho0;
+    ph.cfm = p.cfm_epsilon;
+    ph.corr_n = p.corr_n;
+    const float dq = p.corr_delta_q * h;
+    const float t = hh - dq * dq;
+    ph.corr_wdq = t * t * t;
+    {
+        // poly6(dq) exactly as the oracle's orc_poly6 evaluates it
+        const float f = 315.f / (64.f * kPi * (hhh * hhh * hhh));
+        const float tt = hh - dq * dq;
+        ph.corr_ref = (dq <= h) ? f * (tt * tt * tt) : 0.f;
+    }
+    ph.corr_k = p.profile == FGB_PROFILE_REF ? p.corr_k : p.corr_k * hh;
+    ph.xsph_c = p.xsph_c;
+    ph.vort_eps = p.vorticity_epsilon;
+    ph.damping = p.velocity_damping;
+    ph.mc_size = p.mc_particle_size;
+    ph.mc_infl = p.mc_particle_influence;
+    ph.profile = p.profile;
+    return ph;
+}
+
+// Grid and lattice geometry of one scene (same float operations as the oracle).
+void scene_geometry(const fgb_params &p, const fgb_config &c, SceneDev &S) {
+    const float pad = p.h * 2.f;
+    for (int a = 0; a < 3; ++a) {
+        const float mn = (c.min_bound[a] / c.scale) - pad;
+        const float mx = (c.max_bound[a] / c.scale) + pad;
+        S.min_ext[a] = mn;
+        const float e = (mx - mn) / p.h;
+        uint32_t ei = e > 0.f ? (uint32_t)e : 0u;
+        if (ei > 1023u) ei = 1023u;
+        S.ext[a] = ei;
+    }
+    S.dt = c.dt;
+    S.inv_dt = 1.f / c.dt;
+    S.scale = c.scale;
+    for (int a = 0; a < 3; ++a) {
+        S.g[a] = c.constant_force[a];
+        S.min_b[a] = c.min_bound[a];
+        S.max_b[a] = c.max_bound[a];
+    }
+    S.sphere_enabled = c.sphere_enabled;
+    for (int a = 0; a < 4; ++a) S.sphere[a] = c.sphere[a];
+    S.resolution = c.resolution;
+    S.iso = c.isolevel;
+    const float step = c.resolution > 0.f ? p.h / c.resolution : 0.f;
+    S.lat_step = step;
+    for (int a = 0; a < 3; ++a) {
+        if (c.resolution <= 0.f) {
+            S.lat[a] = 0;
+            S.lat_origin[a] = 0.f;
+        } else if (p.profile == FGB_PROFILE_REF) {
+            S.lat_origin[a] = S.min_ext[a];
+            S.lat[a] = (uint32_t)floorf((float)S.ext[a] * c.resolution) + 1u;
+        } else {
+            const float lo = c.min_bound[a] / c.scale, hi = c.max_bound[a] / c.scale;
+            S.lat_origin[a] = lo;
+            S.lat[a] = (uint32_t)floorf((hi - lo) / step + 0.5f) + 1u;
+        }
+    }
+}
+
+std::once_flag g_tables_once[64];
+
+void ensure_tables() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::call_once(g_tables_once[dev & 63], [] { mc_tables_upload(); });
+}
+
+}  // namespace
+}  // namespace fgb
+
+using namespace fgb;
+
+struct fgb_solver {
+    fgb_params params;
+    Phys ph;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int block = 128;
+    fgb_batch *cached = nullptr;  // single-scene batch behind fgb_advance
+    uint64_t cached_n = 0;
+    fgb_config cached_cfg{};
+    std::vector<TriDev> cached_tris;
+};
+
+struct fgb_batch {
+    fgb_solver *solver = nullptr;
+    uint32_t n_scenes = 0;
+    std::vector<fgb_config> cfg;
+    std::vector<uint64_t> counts, first;
+    uint64_t n = 0;
+    uint32_t mbits = 0, sbits = 0, key_bits = 0, iterations = 0;
+    std::vector<SceneDev> h_scenes;
+    Dev<SceneDev> d_scenes;
+    Dev<WellDev> d_wells;
+    Dev<TriDev> d_tris;
+    std::vector<std::vector<TriDev>> scene_tris;
+    bool tris_dirty = false;
+    Phys ph;
+    // state
+    Dev<float4> x[2], v[2];
+    Dev<int32_t> type[2];
+    Dev<uint32_t> col[2], slot[2];
+    int cur = 0;
+    // step
+    Dev<uint32_t> keys_in, vals_in, keys_sorted, vals_sorted;
+    Dev<char> sort_scratch;
+    uint64_t sort_scratch_bytes = 0;
+    Dev<uint2> cells;
+    uint64_t cells_n = 0;
+    Dev<float4> ps[2];
+    Dev<float> lambda, density;
+    Dev<float4> omega, vx;
+    Dev<uint32_t> err;
+    // surface
+    bool surf_ready = false;
+    uint64_t lat_total = 0, cube_total = 0;
+    Dev<uint32_t> mc_keys, mc_vals;
+    Dev<float4> mc_xs;
+    Dev<int32_t> mc_type;
+    Dev<uint32_t> mc_col;
+    Dev<float4> lattice;
+    Dev<uint32_t> lattice_col;
+    Dev<uint8_t> cases;
+    Dev<uint32_t> offsets;
+    Dev<uint32_t> total;
+    Dev<char> scan_scratch;
+    uint64_t scan_scratch_bytes = 0;
+    Dev<fgb_mesh_triangle> tris_out;
+    uint32_t surf_scene_begin = 0, surf_scene_end = 0;
+    std::vector<uint64_t> surf_tri_first;  // per scene of the last surface_all
+    // host
+    std::vector<std::vector<uint64_t>> ids;
+    Pinned<float4> st_x, st_v;
+    Pinned<int32_t> st_type;
+    Pinned<uint32_t> st_col, st_slot, st_keys;
+    uint64_t launches = 0;
+    uint64_t launches_per_step = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool graphs_ok = false;
+
+    ~fgb_batch() {
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g);
+    }
+
+    cudaStream_t stream() const { return solver->stream; }
+
+    StepView view(int c) {
+        StepView s{};
+        s.scenes = d_scenes.p;
+        s.wells = d_wells.p;
+        s.tris = d_tris.p;
+        s.n = (uint32_t)n;
+        s.mbits = mbits;
+        s.ph = ph;
+        s.x0 = x[c].p;
+        s.v0 = v[c].p;
+        s.type0 = type[c].p;
+        s.col0 = col[c].p;
+        s.slot0 = slot[c].p;
+        s.x1 = x[c ^ 1].p;
+        s.v1 = v[c ^ 1].p;
+        s.type1 = type[c ^ 1].p;
+        s.col1 = col[c ^ 1].p;
+        s.slot1 = slot[c ^ 1].p;
+        s.keys_prev = keys_sorted.p;
+        s.keys_in = keys_in.p;
+        s.vals_in = vals_in.p;
+        s.keys_sorted = keys_sorted.p;
+        s.vals_sorted = vals_sorted.p;
+        s.cells = cells.p;
+        s.cells_n = cells_n;
+        s.ps_a = ps[0].p;
+        s.ps_b = ps[1].p;
+        s.lambda = lambda.p;
+        s.density = density.p;
+        s.omega = omega.p;
+        s.vx = vx.p;
+        s.err = err.p;
+        s.block = solver->block;
+        return s;
+    }
+
+    // Enqueue one step that reads state set c and leaves the state in set c^1.
+    int record_step(int c) {
+        cudaStream_t st = stream();
+        StepView s = view(c);
+        uint64_t l = 0;
+        launch_predict_keys(s, st);
+        l += 1;
+        cudaError_t e = radix_sort_pairs(keys_in.p, vals_in.p, keys_sorted.p, vals_sorted.p, n, key_bits,
+                                         sort_scratch.p, sort_scratch_bytes, st, err.p, &l);
+        if (e != cudaSuccess) return fail_cuda(e, "step: radix sort");
+        FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
+        launch_reorder_cells(s, st);
+        l += 1;
+        for (uint32_t it = 0; it < iterations; ++it) {
+            const float4 *pin = ps[it & 1].p;
+            float4 *pout = ps[(it + 1) & 1].p;
+            launch_lambda(s, pin, st);
+            launch_delta(s, pin, pout, it + 1 == iterations, st);
+            l += 2;
+        }
+        if (ph.profile != FGB_PROFILE_REF) {
+            launch_velocity_terms(s, ps[iterations & 1].p, st);
+            l += 2;
+        }
+        FGB_CUDA(cudaGetLastError(), "step: launch");
+        launches_per_step = l;
+        return FGB_OK;
+    }
+
+    int sync_tris() {
+        if (!tris_dirty) return FGB_OK;
+        std::vector<TriDev> all;
+        for (uint32_t k = 0; k < n_scenes; ++k) {
+            h_scenes[k].tri_first = (uint32_t)all.size();
+            h_scenes[k].tri_count = (uint32_t)scene_tris[k].size();
+            all.insert(all.end(), scene_tris[k].begin(), scene_tris[k].end());
+        }
+        bool moved = false;
+        if (all.size() > d_tris.n || !d_tris.p) {
+            FGB_CUDA(d_tris.alloc(std::max<size_t>(all.size(), 1)), "colliders");
+            moved = true;
+        }
+        if (!all.empty())
+            FGB_CUDA(cudaMemcpyAsync(d_tris.p, all.data(), all.size() * sizeof(TriDev), cudaMemcpyHostToDevice,
+                                     stream()),
+                     "colliders upload");
+        FGB_CUDA(cudaMemcpyAsync(d_scenes.p, h_scenes.data(), n_scenes * sizeof(SceneDev), cudaMemcpyHostToDevice,
+                                 stream()),
+                 "scene upload");
+        FGB_CUDA(cudaStreamSynchronize(stream()), "colliders sync");
+        tris_dirty = false;
+        if (moved) {  // the collider array pointer is baked into the graphs
+            for (auto &g : graph)
+                if (g) cudaGraphExecDestroy(g), g = nullptr;
+            graphs_ok = false;
+        }
+        return FGB_OK;
+    }
+
+    int build_graphs() {
+        cudaStream_t st = stream();
+        for (int c = 0; c < 2; ++c) {
+            cudaGraph_t g = nullptr;
+            FGB_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+            int rc = record_step(c);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc != FGB_OK) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return fail_cuda(e, "graph capture end");
+            e = cudaGraphInstantiate(&graph[c], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail_cuda(e, "graph instantiate");
+        }
+        graphs_ok = true;
+        return FGB_OK;
+    }
+
+    int step(uint32_t steps) {
+        int rc = sync_tris();
+        if (rc) return rc;
+        if (!graphs_ok) {
+            rc = build_graphs();
+            if (rc) return rc;
+        }
+        for (uint32_t k = 0; k < steps; ++k) {
+            FGB_CUDA(cudaGraphLaunch(graph[cur], stream()), "graph launch");
+            cur ^= 1;
+            launches += launches_per_step;
+        }
+        return FGB_OK;
+    }
+
+    int ensure_surface() {
+        if (surf_ready) return FGB_OK;
+        FGB_CUDA(mc_keys.alloc(n), "surface alloc");
+        FGB_CUDA(mc_vals.alloc(n), "surface alloc");
+        FGB_CUDA(mc_xs.alloc(n), "surface alloc");
+        FGB_CUDA(mc_type.alloc(n), "surface alloc");
+        FGB_CUDA(mc_col.alloc(n), "surface alloc");
+        FGB_CUDA(lattice.alloc(lat_total), "surface alloc lattice");
+        FGB_CUDA(lattice_col.alloc(lat_total), "surface alloc lattice");
+        FGB_CUDA(cases.alloc(cube_total), "surface alloc cubes");
+        FGB_CUDA(offsets.alloc(cube_total + 1), "surface alloc cubes");
+        FGB_CUDA(total.alloc(1), "surface alloc");
+        scan_scratch_bytes = scan_u32_scratch_bytes(cube_total);
+        FGB_CUDA(scan_scratch.alloc(scan_scratch_bytes), "surface alloc");
+        surf_ready = true;
+        return FGB_OK;
+    }
+
+    // Grid over the current positions, then field + classify + scan for scenes [b, e).
+    int surface_count(uint32_t b, uint32_t e, uint64_t *tri_total) {
+        int rc = ensure_surface();
+        if (rc) return rc;
+        cudaStream_t st = stream();
+        StepView s = view(cur);
+        s.keys_prev = keys_sorted.p;
+        launch_position_keys(s, x[cur].p, st);
+        launches += 1;
+        cudaError_t ce = radix_sort_pairs(keys_in.p, vals_in.p, mc_keys.p, mc_vals.p, n, key_bits, sort_scratch.p,
+                                          sort_scratch_bytes, st, err.p, &launches);
+        if (ce != cudaSuccess) return fail_cuda(ce, "surface: sort");
+        FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "surface: clear cells");
+        s.keys_sorted = mc_keys.p;
+        s.vals_sorted = mc_vals.p;
+        launch_gather_positions(s, x[cur].p, type[cur].p, col[cur].p, mc_xs.p, mc_type.p, mc_col.p, st);
+        launches += 1;
+        SurfaceView v = surface_view(b, e);
+        ce = launch_surface_count(v, st, &launches);
+        if (ce != cudaSuccess) return fail_cuda(ce, "surface: count");
+        uint32_t t = 0;
+        FGB_CUDA(cudaMemcpyAsync(&t, total.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "surface: total");
+        FGB_CUDA(cudaStreamSynchronize(st), "surface: sync");
+        *tri_total = t;
+        surf_scene_begin = b;
+        surf_scene_end = e;
+        return FGB_OK;
+    }
+
+    SurfaceView surface_view(uint32_t b, uint32_t e) {
+        SurfaceView v{};
+        v.scenes = d_scenes.p;
+        v.h_scenes = h_scenes.data();
+        v.scene_begin = b;
+        v.scene_end = e;
+        v.mbits = mbits;
+        v.ph = ph;
+        v.keys_sorted = mc_keys.p;
+        v.cells = cells.p;
+        v.xs = mc_xs.p;
+        v.type = mc_type.p;
+        v.col = mc_col.p;
+        v.lattice = lattice.p;
+        v.lattice_col = lattice_col.p;
+        v.cases = cases.p;
+        v.offsets = offsets.p;
+        v.total = total.p;
+        v.lat_begin = h_scenes[b].lat_base;
+        v.lat_end = (e < n_scenes) ? h_scenes[e].lat_base : lat_total;
+        v.cube_begin = h_scenes[b].cube_base;
+        v.cube_end = (e < n_scenes) ? h_scenes[e].cube_base : cube_total;
+        v.scan_scratch = scan_scratch.p;
+        v.scan_scratch_bytes = scan_scratch_bytes;
+        v.err = err.p;
+        return v;
+    }
+
+    int surface_emit(uint64_t tri_total) {
+        if (tri_total > tris_out.n || !tris_out.p) {
+            uint64_t cap = std::max<uint64_t>(tri_total + tri_total / 4, 1024);
+            FGB_CUDA(tris_out.alloc(cap), "surface: triangles alloc");
+        }
+        SurfaceView v = surface_view(surf_scene_begin, surf_scene_end);
+        cudaError_t ce = launch_surface_emit(v, tris_out.p, tris_out.n, stream(), &launches);
+        if (ce != cudaSuccess) return fail_cuda(ce, "surface: emit");
+        return FGB_OK;
+    }
+};
+
+static int mesh_assign(fgb_mesh *m, const fgb_mesh_triangle *dev, uint64_t count, cudaStream_t st) {
+    if (!m) return FGB_OK;
+    if (count > m->capacity || !m->triangles) {
+        free(m->triangles);
+        m->triangles = (fgb_mesh_triangle *)malloc(std::max<uint64_t>(count, 1) * sizeof(fgb_mesh_triangle));
+        if (!m->triangles) {
+            m->capacity = 0;
+            m->n = 0;
+            return fail(FGB_ERR_OOM, "mesh: host allocation failed");
+        }
+        m->capacity = std::max<uint64_t>(count, 1);
+    }
+    m->n = count;
+    if (count)
+        FGB_CUDA(cudaMemcpyAsync(m->triangles, dev, count * sizeof(fgb_mesh_triangle), cudaMemcpyDeviceToHost, st),
+                 "mesh: copy");
+    FGB_CUDA(cudaStreamSynchronize(st), "mesh: sync");
+    return FGB_OK;
+}
+
+static int batch_init(fgb_batch *b) {
+    fgb_solver *s = b->solver;
+    const fgb_params &p = s->params;
+    b->ph = s->ph;
+    b->h_scenes.assign(b->n_scenes, SceneDev{});
+    uint32_t max_ext = 0;
+    uint64_t table = 0, lat = 0, cubes = 0;
+    std::vector<WellDev> wells;
+    b->first.resize(b->n_scenes);
+    uint64_t off = 0;
+    b->iterations = b->cfg[0].iterations;
+    for (uint32_t k = 0; k < b->n_scenes; ++k) {
+        const fgb_config &c = b->cfg[k];
+        if (!(c.scale > 0.f) || !(c.dt > 0.f)) return fail(FGB_ERR_INVALID, "config: scale and dt must be > 0");
+        if (c.iterations != b->iterations)
+            return fail(FGB_ERR_INVALID, "batch: every scene needs the same iteration count");
+        if (c.n_wells > FGB_MAX_WELLS) return fail(FGB_ERR_CAPACITY, "config: more than FGB_MAX_WELLS wells");
+        for (int a = 0; a < 3; ++a)
+            if (!(c.max_bound[a] >= c.min_bound[a])) return fail(FGB_ERR_INVALID, "config: max_bound < min_bound");
+        SceneDev &S = b->h_scenes[k];
+        scene_geometry(p, c, S);
+        for (int a = 0; a < 3; ++a) max_ext = std::max(max_ext, S.ext[a]);
+        S.table_base = (uint32_t)table;
+        table += (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
+        S.first = (uint32_t)off;
+        S.count = (uint32_t)b->counts[k];
+        b->first[k] = off;
+        off += b->counts[k];
+        S.n_wells = c.n_wells;
+        S.well_first = (uint32_t)wells.size();
+        for (uint32_t w = 0; w < c.n_wells; ++w) {
+            WellDev wd;
+            for (int a = 0; a < 3; ++a) wd.centre[a] = c.wells[w].centre[a];
+            wd.force = c.wells[w].force;
+            wells.push_back(wd);
+        }
+        S.lat_base = lat;
+        S.cube_base = cubes;
+        lat += (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];
+        if (S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1)
+            cubes += (uint64_t)(S.lat[0] - 1) * (S.lat[1] - 1) * (S.lat[2] - 1);
+    }
+    if (b->iterations == 0) return fail(FGB_ERR_INVALID, "config: iterations must be >= 1");
+    b->n = off;
+    if (b->n > 0x7fffffffull) return fail(FGB_ERR_CAPACITY, "batch: more than 2^31-1 particles");
+    if (table > 0xffffffffull) return fail(FGB_ERR_CAPACITY, "batch: cell tables above 2^32 entries");
+    b->cells_n = table;
+    b->lat_total = lat;
+    b->cube_total = cubes;
+    if (cubes > 0xffffffffull) return fail(FGB_ERR_CAPACITY, "batch: more than 2^32-1 marching cubes");
+    b->mbits = 3 * bits_for(max_ext);
+    b->sbits = bits_for(b->n_scenes - 1);
+    b->key_bits = b->mbits + b->sbits;
+    if (b->key_bits > 32) return fail(FGB_ERR_CAPACITY, "batch: scene id + Morton key exceed 32 bits");
+    if (b->key_bits == 0) b->key_bits = 1;
+    const uint64_t n = std::max<uint64_t>(b->n, 1);
+    ensure_tables();
+    for (int c = 0; c < 2; ++c) {
+        FGB_CUDA(b->x[c].alloc(n), "batch alloc");
+        FGB_CUDA(b->v[c].alloc(n), "batch alloc");
+        FGB_CUDA(b->type[c].alloc(n), "batch alloc");
+        FGB_CUDA(b->col[c].alloc(n), "batch alloc");
+        FGB_CUDA(b->slot[c].alloc(n), "batch alloc");
+        FGB_CUDA(b->ps[c].alloc(n), "batch alloc");
+    }
+    FGB_CUDA(b->keys_in.alloc(n), "batch alloc");
+    FGB_CUDA(b->vals_in.alloc(n), "batch alloc");
+    FGB_CUDA(b->keys_sorted.alloc(n), "batch alloc");
+    FGB_CUDA(b->vals_sorted.alloc(n), "batch alloc");
+    b->sort_scratch_bytes = radix_scratch_bytes(n);
+    FGB_CUDA(b->sort_scratch.alloc(b->sort_scratch_bytes), "batch alloc");
+    FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
+    FGB_CUDA(b->lambda.alloc(n), "batch alloc");
+    FGB_CUDA(b->density.alloc(n), "batch alloc");
+    if (p.profile != FGB_PROFILE_REF) {
+        FGB_CUDA(b->omega.alloc(n), "batch alloc");
+        FGB_CUDA(b->vx.alloc(n), "batch alloc");
+    }
+    FGB_CUDA(b->err.alloc(1), "batch alloc");
+    FGB_CUDA(b->d_scenes.alloc(b->n_scenes), "batch alloc");
+    FGB_CUDA(b->d_wells.alloc(std::max<size_t>(wells.size(), 1)), "batch alloc");
+    FGB_CUDA(b->d_tris.alloc(1), "batch alloc");
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), st), "batch init");
+    FGB_CUDA(cudaMemsetAsync(b->lambda.p, 0, n * sizeof(float), st), "batch init");
+    FGB_CUDA(cudaMemsetAsync(b->density.p, 0, n * sizeof(float), st), "batch init");
+    if (!wells.empty())
+        FGB_CUDA(cudaMemcpyAsync(b->d_wells.p, wells.data(), wells.size() * sizeof(WellDev), cudaMemcpyHostToDevice, st),
+                 "batch init");
+    FGB_CUDA(cudaMemcpyAsync(b->d_scenes.p, b->h_scenes.data(), b->n_scenes * sizeof(SceneDev),
+                             cudaMemcpyHostToDevice, st),
+             "batch init");
+    // scene ids in the high key bits before the first step
+    FGB_CUDA(b->st_keys.ensure(n), "batch init");
+    for (uint32_t k = 0; k < b->n_scenes; ++k)
+        for (uint64_t i = 0; i < b->counts[k]; ++i)
+            b->st_keys.p[b->first[k] + i] = b->mbits >= 32 ? 0u : (k << b->mbits);
+    FGB_CUDA(cudaMemcpyAsync(b->keys_sorted.p, b->st_keys.p, b->n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+             "batch init");
+    FGB_CUDA(cudaStreamSynchronize(st), "batch init");
+    b->ids.assign(b->n_scenes, {});
+    b->scene_tris.assign(b->n_scenes, {});
+    return FGB_OK;
+}
+
+static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
+    if (k >= b->n_scenes) return fail(FGB_ERR_INVALID, "upload: scene out of range");
+    if (!xs || xs->n != b->counts[k]) return fail(FGB_ERR_INVALID, "upload: particle count differs from the batch");
+    const uint64_t n = xs->n, f = b->first[k];
+    if (n && (!xs->position || !xs->velocity || !xs->mass || !xs->type))
+        return fail(FGB_ERR_INVALID, "upload: null particle array");
+    FGB_CUDA(b->st_x.ensure(n), "upload staging");
+    FGB_CUDA(b->st_v.ensure(n), "upload staging");
+    FGB_CUDA(b->st_type.ensure(n), "upload staging");
+    FGB_CUDA(b->st_col.ensure(n), "upload staging");
+    FGB_CUDA(b->st_slot.ensure(n), "upload staging");
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
+    for (uint64_t i = 0; i < n; ++i) {
+        b->st_x.p[i] = make_float4(xs->position[3 * i], xs->position[3 * i + 1], xs->position[3 * i + 2], xs->mass[i]);
+        b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
+        b->st_type.p[i] = xs->type[i];
+        b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
+        b->st_slot.p[i] = (uint32_t)i;
+    }
+    b->ids[k].assign(n, 0);
+    for (uint64_t i = 0; i < n; ++i) b->ids[k][i] = xs->id ? xs->id[i] : i;
+    const int c = b->cur;
+    if (n) {
+        FGB_CUDA(cudaMemcpyAsync(b->x[c].p + f, b->st_x.p, n * sizeof(float4), cudaMemcpyHostToDevice, st), "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->v[c].p + f, b->st_v.p, n * sizeof(float4), cudaMemcpyHostToDevice, st), "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->type[c].p + f, b->st_type.p, n * sizeof(int32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->col[c].p + f, b->st_col.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->slot[c].p + f, b->st_slot.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+    }
+    // the scene's key prefix, in case a surface call precedes the first step
+    FGB_CUDA(b->st_keys.ensure(n), "upload staging");
+    for (uint64_t i = 0; i < n; ++i) b->st_keys.p[i] = b->mbits >= 32 ? 0u : (k << b->mbits);
+    if (n)
+        FGB_CUDA(cudaMemcpyAsync(b->keys_sorted.p + f, b->st_keys.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+    FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
+    return FGB_OK;
+}
+
+static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
+    if (k >= b->n_scenes) return fail(FGB_ERR_INVALID, "download: scene out of range");
+    if (!xs || xs->n != b->counts[k]) return fail(FGB_ERR_INVALID, "download: particle count differs");
+    const uint64_t n = xs->n, f = b->first[k];
+    FGB_CUDA(b->st_x.ensure(n), "download staging");
+    FGB_CUDA(b->st_v.ensure(n), "download staging");
+    FGB_CUDA(b->st_type.ensure(n), "download staging");
+    FGB_CUDA(b->st_col.ensure(n), "download staging");
+    FGB_CUDA(b->st_slot.ensure(n), "download staging");
+    cudaStream_t st = b->stream();
+    const int c = b->cur;
+    if (n) {
+        FGB_CUDA(cudaMemcpyAsync(b->st_x.p, b->x[c].p + f, n * sizeof(float4), cudaMemcpyDeviceToHost, st), "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_v.p, b->v[c].p + f, n * sizeof(float4), cudaMemcpyDeviceToHost, st), "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_type.p, b->type[c].p + f, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
+                 "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_col.p, b->col[c].p + f, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                 "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_slot.p, b->slot[c].p + f, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                 "download");
+    }
+    FGB_CUDA(cudaStreamSynchronize(st), "download sync");
+    const std::vector<uint64_t> &ids = b->ids[k];
+    for (uint64_t i = 0; i < n; ++i) {
+        const float4 X = b->st_x.p[i], V = b->st_v.p[i];
+        if (xs->position) {
+            xs->position[3 * i] = X.x;
+            xs->position[3 * i + 1] = X.y;
+            xs->position[3 * i + 2] = X.z;
+        }
+        if (xs->mass) xs->mass[i] = X.w;
+        if (xs->velocity) {
+            xs->velocity[3 * i] = V.x;
+            xs->velocity[3 * i + 1] = V.y;
+            xs->velocity[3 * i + 2] = V.z;
+        }
+        if (xs->type) xs->type[i] = b->st_type.p[i];
+        if (xs->colour) xs->colour[i] = b->st_col.p[i];
+        const uint32_t sl = b->st_slot.p[i];
+        if (xs->id) xs->id[i] = sl < ids.size() ? ids[sl] : sl;
+    }
+    return FGB_OK;
+}
+
+static void destroy_batch(fgb_batch *b) { delete b; }
+
+extern "C" {
+
+int fgb_version(void) { return FGB_VERSION; }
+
+const char *fgb_last_error(void) { return g_last_error.c_str(); }
+
+int fgb_struct_sizes(uint64_t *out, int n) {
+    const uint64_t sizes[] = {sizeof(fgb_params), sizeof(fgb_config),        sizeof(fgb_particles),
+                              sizeof(fgb_triangle), sizeof(fgb_mesh_triangle), sizeof(fgb_mesh),
+                              sizeof(fgb_grid_info), sizeof(fgb_well)};
+    const int m = (int)(sizeof(sizes) / sizeof(sizes[0]));
+    for (int i = 0; i < n && i < m; ++i) out[i] = sizes[i];
+    return m;
+}
+
+void fgb_params_default(fgb_params *p, int32_t profile, float h) {
+    if (!p) return;
+    memset(p, 0, sizeof *p);
+    p->h = h;
+    p->profile = profile;
+    p->corr_n = 4.f;
+    p->mc_particle_size = 25.f;     // oclsph.hpp:672
+    p->mc_particle_influence = 0.5f; // oclsph.hpp:673
+    p->vorticity_epsilon = 0.0005f;  // oclsph_kernel.h:29
+    if (profile == FGB_PROFILE_REF) { // oclsph_kernel.h:20-31
+        p->rho0 = 6378.f;
+        p->cfm_epsilon = 600.f;
+        p->corr_k = 0.0001f;
+        p->corr_delta_q = 0.3f;
+        p->xsph_c = 0.00001f;
+        p->velocity_damping = 0.49f;
+    } else {
+        p->rho0 = 1000.f;
+        p->cfm_epsilon = 100.f;
+        p->corr_k = 0.1f;
+        p->corr_delta_q = 0.2f;
+        p->xsph_c = 0.01f;
+        p->velocity_damping = 1.f;
+    }
+}
+
+void fgb_config_default(fgb_config *c, int32_t profile) {
+    if (!c) return;
+    memset(c, 0, sizeof *c);
+    c->scale = 1.f;
+    c->resolution = 2.f;
+    if (profile == FGB_PROFILE_REF) {
+        // samples/main.cpp:398-404 (solverStep 1, isolevel 100, gravity along y)
+        c->dt = 0.0083f;
+        c->isolevel = 100.f;
+        c->iterations = 5;
+        c->constant_force[1] = 9.8f;
+        c->surface = 1;
+    } else {
+        c->dt = 1.f / 120.f;
+        c->isolevel = 500.f;
+        c->iterations = 4;
+        c->constant_force[1] = -9.81f;
+    }
+    for (int a = 0; a < 3; ++a) c->max_bound[a] = 1.f;
+}
+
+int fgb_create(const fgb_params *params, fgb_solver **out) {
+    if (!params || !out) return fail(FGB_ERR_INVALID, "create: null argument");
+    if (!(params->h > 0.f)) return fail(FGB_ERR_INVALID, "create: h must be > 0");
+    if (params->profile != FGB_PROFILE_REF && params->profile != FGB_PROFILE_BASELINE)
+        return fail(FGB_ERR_INVALID, "create: unknown profile");
+    if (!(params->rho0 > 0.f)) return fail(FGB_ERR_INVALID, "create: rho0 must be > 0");
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return fail(FGB_ERR_CUDA, "create: no CUDA device (this library has no CPU fallback)");
+    fgb_solver *s = new fgb_solver();
+    s->params = *params;
+    s->ph = make_phys(*params);
+    cudaGetDevice(&s->device);
+    e = cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail_cuda(e, "create: stream");
+    }
+    s->stream = s->own;
+    ensure_tables();
+    *out = s;
+    return FGB_OK;
+}
+
+int fgb_destroy(fgb_solver *s) {
+    if (!s) return FGB_OK;
+    if (s->cached) destroy_batch(s->cached);
+    if (s->own) {
+        cudaStreamSynchronize(s->own);
+        cudaStreamDestroy(s->own);
+    }
+    delete s;
+    return FGB_OK;
+}
+
+int fgb_set_stream(fgb_solver *s, void *cuda_stream) {
+    if (!s) return fail(FGB_ERR_INVALID, "set_stream: null solver");
+    cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : s->own;
+    if (st == s->stream) return FGB_OK;
+    s->stream = st;
+    if (s->cached) {
+        for (auto &g : s->cached->graph)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        s->cached->graphs_ok = false;
+    }
+    return FGB_OK;
+}
+
+int fgb_batch_create(fgb_solver *s, uint32_t n_scenes, const uint64_t *counts, const fgb_config *configs,
+                     fgb_batch **out) {
+    if (!s || !counts || !configs || !out || n_scenes == 0) return fail(FGB_ERR_INVALID, "batch_create: bad argument");
+    fgb_batch *b = new fgb_batch();
+    b->solver = s;
+    b->n_scenes = n_scenes;
+    b->counts.assign(counts, counts + n_scenes);
+    b->cfg.assign(configs, configs + n_scenes);
+    int rc = batch_init(b);
+    if (rc != FGB_OK) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return FGB_OK;
+}
+
+int fgb_batch_destroy(fgb_batch *b) {
+    if (!b) return FGB_OK;
+    cudaStreamSynchronize(b->stream());
+    destroy_batch(b);
+    return FGB_OK;
+}
+
+int fgb_batch_upload(fgb_batch *b, uint32_t scene, const fgb_particles *xs) {
+    if (!b) return fail(FGB_ERR_INVALID, "upload: null batch");
+    return batch_upload(b, scene, xs);
+}
+
+int fgb_batch_set_colliders(fgb_batch *b, uint32_t scene, const fgb_triangle *tris, size_t n) {
+    if (!b || scene >= b->n_scenes || (n && !tris)) return fail(FGB_ERR_INVALID, "set_colliders: bad argument");
+    std::vector<TriDev> t(n);
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            t[i].a[a] = tris[i].a[a];
+            t[i].b[a] = tris[i].b[a];
+            t[i].c[a] = tris[i].c[a];
+        }
+    std::vector<TriDev> &old = b->scene_tris[scene];
+    if (old.size() == t.size() && (t.empty() || memcmp(old.data(), t.data(), t.size() * sizeof(TriDev)) == 0))
+        return FGB_OK;
+    old.swap(t);
+    b->tris_dirty = true;
+    return FGB_OK;
+}
+
+int fgb_batch_step(fgb_batch *b, uint32_t steps) {
+    if (!b) return fail(FGB_ERR_INVALID, "step: null batch");
+    if (b->n == 0) return FGB_OK;
+    return b->step(steps);
+}
+
+int fgb_batch_download(fgb_batch *b, uint32_t scene, fgb_particles *xs) {
+    if (!b) return fail(FGB_ERR_INVALID, "download: null batch");
+    return batch_download(b, scene, xs);
+}
+
+int fgb_batch_surface(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out) {
+    if (!b || scene >= b->n_scenes) return fail(FGB_ERR_INVALID, "surface: bad argument");
+    if (b->h_scenes[scene].lat[0] < 2) {
+        if (mesh_out) mesh_out->n = 0;
+        return FGB_OK;
+    }
+    uint64_t t = 0;
+    int rc = b->surface_count(scene, scene + 1, &t);
+    if (rc) return rc;
+    rc = b->surface_emit(t);
+    if (rc) return rc;
+    return mesh_assign(mesh_out, b->tris_out.p, t, b->stream());
+}
+
+int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts) {
+    if (!b) return fail(FGB_ERR_INVALID, "surface_all: null batch");
+    uint64_t t = 0;
+    int rc = b->surface_count(0, b->n_scenes, &t);
+    if (rc) return rc;
+    rc = b->surface_emit(t);
+    if (rc) return rc;
+    // per-scene triangle ranges: offsets at each scene's first cube
+    std::vector<uint32_t> firsts(b->n_scenes);
+    b->surf_tri_first.assign(b->n_scenes + 1, 0);
+    cudaStream_t st = b->stream();
+    for (uint32_t k = 0; k < b->n_scenes; ++k) {
+        const uint64_t cb = b->h_scenes[k].cube_base;
+        if (cb < b->cube_total)
+            FGB_CUDA(cudaMemcpyAsync(&firsts[k], b->offsets.p + cb, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                     "surface_all: offsets");
+        else
+            firsts[k] = (uint32_t)t;
+    }
+    FGB_CUDA(cudaStreamSynchronize(st), "surface_all: sync");
+    for (uint32_t k = 0; k < b->n_scenes; ++k) b->surf_tri_first[k] = firsts[k];
+    b->surf_tri_first[b->n_scenes] = t;
+    for (uint32_t k = 0; k < b->n_scenes; ++k)
+        if (counts) counts[k] = b->surf_tri_first[k + 1] - b->surf_tri_first[k];
+    return FGB_OK;
+}
+
+int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out) {
+    if (!b || scene >= b->n_scenes || b->surf_tri_first.size() != b->n_scenes + 1)
+        return fail(FGB_ERR_INVALID, "surface_fetch: call fgb_batch_surface_all first");
+    const uint64_t f = b->surf_tri_first[scene], e = b->surf_tri_first[scene + 1];
+    return mesh_assign(mesh_out, b->tris_out.p + f, e - f, b->stream());
+}
+
+int fgb_batch_sync(fgb_batch *b) {
+    if (!b) return fail(FGB_ERR_INVALID, "sync: null batch");
+    FGB_CUDA(cudaStreamSynchronize(b->stream()), "sync");
+    return FGB_OK;
+}
+
+int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
+    if (!b || !flags) return fail(FGB_ERR_INVALID, "error_flags: bad argument");
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemcpyAsync(flags, b->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "error_flags");
+    FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), st), "error_flags");
+    FGB_CUDA(cudaStreamSynchronize(st), "error_flags");
+    return FGB_OK;
+}
+
+uint64_t fgb_batch_launch_count(const fgb_batch *b) { return b ? b->launches : 0; }
+
+int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes) {
+    if (!b || !bytes) return fail(FGB_ERR_INVALID, "probe: bad argument");
+    const uint64_t n = b->n;
+    switch (what) {
+    case FGB_PROBE_KEYS:
+    case FGB_PROBE_ORDER:
+    case FGB_PROBE_LAMBDA:
+    case FGB_PROBE_DENSITY: *bytes = n * 4; break;
+    case FGB_PROBE_CELLS: *bytes = b->cells_n * 8; break;
+    case FGB_PROBE_LATTICE: *bytes = b->lat_total * 16; break;
+    case FGB_PROBE_CUBE_CASES: *bytes = b->cube_total; break;
+    default: return fail(FGB_ERR_INVALID, "probe: unknown array");
+    }
+    return FGB_OK;
+}
+
+int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes) {
+    uint64_t want = 0;
+    int rc = fgb_batch_probe_size(b, what, &want);
+    if (rc) return rc;
+    if (bytes != want || (!host_out && bytes)) return fail(FGB_ERR_INVALID, "probe: wrong size");
+    const void *src = nullptr;
+    switch (what) {
+    case FGB_PROBE_KEYS: src = b->keys_sorted.p; break;
+    case FGB_PROBE_ORDER: src = b->slot[b->cur].p; break;
+    case FGB_PROBE_LAMBDA: src = b->lambda.p; break;
+    case FGB_PROBE_DENSITY: src = b->density.p; break;
+    case FGB_PROBE_CELLS: src = b->cells.p; break;
+    case FGB_PROBE_LATTICE: src = b->lattice.p; break;
+    case FGB_PROBE_CUBE_CASES: src = b->cases.p; break;
+    }
+    if (!src) return fail(FGB_ERR_INVALID, "probe: array not allocated yet");
+    cudaStream_t st = b->stream();
+    if (bytes) FGB_CUDA(cudaMemcpyAsync(host_out, src, bytes, cudaMemcpyDeviceToHost, st), "probe");
+    FGB_CUDA(cudaStreamSynchronize(st), "probe");
+    return FGB_OK;
+}
+
+int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out) {
+    if (!b || !out || scene >= b->n_scenes) return fail(FGB_ERR_INVALID, "grid_info: bad argument");
+    const SceneDev &S = b->h_scenes[scene];
+    for (int a = 0; a < 3; ++a) {
+        out->min_extent[a] = S.min_ext[a];
+        out->extent[a] = S.ext[a];
+        out->lattice[a] = S.lat[a];
+        out->lattice_origin[a] = S.lat_origin[a];
+    }
+    out->table_offset = S.table_base;
+    out->table_size = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
+    out->morton_bits = b->mbits;
+    out->scene_bits = b->sbits;
+    out->lattice_step = S.lat_step;
+    return FGB_OK;
+}
+
+int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const fgb_triangle *colliders,
+                size_t n_colliders, fgb_mesh *mesh_out) {
+    if (!s || !cfg || !xs) return fail(FGB_ERR_INVALID, "advance: null argument");
+    if (n_colliders && !colliders) return fail(FGB_ERR_INVALID, "advance: null colliders");
+    if (mesh_out) mesh_out->n = 0;
+    if (xs->n == 0) return FGB_OK;  // oclsph.hpp:711-715 returns an empty result
+    const bool same = s->cached && s->cached_n == xs->n &&
+                      memcmp(&s->cached_cfg, cfg, sizeof(fgb_config)) == 0;
+    if (!same) {
+        if (s->cached) destroy_batch(s->cached);
+        s->cached = nullptr;
+        uint64_t n = xs->n;
+        int rc = fgb_batch_create(s, 1, &n, cfg, &s->cached);
+        if (rc) return rc;
+        s->cached_n = xs->n;
+        s->cached_cfg = *cfg;
+    }
+    fgb_batch *b = s->cached;
+    int rc = fgb_batch_set_colliders(b, 0, colliders, n_colliders);
+    if (rc) return rc;
+    rc = batch_upload(b, 0, xs);
+    if (rc) return rc;
+    rc = b->step(1);
+    if (rc) return rc;
+    if (cfg->surface && mesh_out) {
+        rc = fgb_batch_surface(b, 0, mesh_out);
+        if (rc) return rc;
+    }
+    return batch_download(b, 0, xs);
+}
+
+void fgb_mesh_free(fgb_mesh *m) {
+    if (!m) return;
+    free(m->triangles);
+    m->triangles = nullptr;
+    m->n = 0;
+    m->capacity = 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+"""Python mirror of libfluid's solver interface over the C ABI.
+
+`SphSolver.advance(config, particles, colliders)` has the meaning of
+fluid::SphSolver<size_t,float>::advance (include/fluid/fluid.hpp:222-232): the
+particles are advanced one step and written back reordered into Morton order,
+and when the config asks for a surface the marching-cubes triangles are
+returned.  Errors raise `capi.FluidError` carrying the library's status code,
+as the reference throws.  There is no CPU fallback: a missing CUDA library or
+device raises.
+"""
+import ctypes
+
+import numpy as np
+
+from . import capi
+
+_P = ctypes.POINTER
+
+
+def _tri_array(colliders):
+    if colliders is None or len(colliders) == 0:
+        return None, 0
+    arr = np.ascontiguousarray(colliders, dtype=np.float32).reshape(-1, 9)
+    return arr, len(arr)
+
+
+class SphSolver:
+    """Replaces ocl::SphSolver(h, kernelPath, device) (include/fluid/oclsph.hpp:170-189)."""
+
+    def __init__(self, h=0.1, profile=capi.PROFILE_BASELINE, params=None):
+        self.lib = capi.load()
+        self.params = params if params is not None else capi.params(profile, h)
+        self._h = ctypes.c_void_p()
+        capi.check(self.lib.fgb_create(ctypes.byref(self.params), ctypes.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        capi.check(self.lib.fgb_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def advance(self, config, particles, colliders=None):
+        """One frame on a dict of numpy arrays (updated in place, Morton order);
+        returns the mesh as an (n, 21) float32 array (v0 v1 v2 n0 n1 n2 + colours as
+        raw uint32 bits) when config.surface is set, else None."""
+        pv = capi.particles_view(particles)
+        tris, ntris = _tri_array(colliders)
+        mesh = capi.Mesh()
+        tp = tris.ctypes.data_as(_P(capi.Triangle)) if tris is not None else None
+        rc = self.lib.fgb_advance(self._h, ctypes.byref(config), ctypes.byref(pv), tp, ntris,
+                                  ctypes.byref(mesh))
+        try:
+            capi.check(rc)
+            return capi.mesh_to_numpy(mesh) if config.surface else None
+        finally:
+            self.lib.fgb_mesh_free(ctypes.byref(mesh))
+
+    def close(self):
+        if self._h:
+            self.lib.fgb_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Resident scenes advanced together (one launch per stage for all scenes)."""
+
+    def __init__(self, solver, scenes):
+        self.solver = solver
+        self.lib = solver.lib
+        self.n_scenes = len(scenes)
+        counts = (ctypes.c_uint64 * self.n_scenes)(*[len(p["mass"]) for p, _ in scenes])
+        cfgs = (capi.Config * self.n_scenes)(*[c for _, c in scenes])
+        self.counts = [int(c) for c in counts]
+        self.configs = [c for _, c in scenes]
+        self._h = ctypes.c_void_p()
+        capi.check(self.lib.fgb_batch_create(solver.handle, self.n_scenes, counts, cfgs, ctypes.byref(self._h)))
+        for k, (parts, _) in enumerate(scenes):
+            self.upload(k, parts)
+
+    def upload(self, k, parts):
+        pv = capi.particles_view(parts)
+        capi.check(self.lib.fgb_batch_upload(self._h, k, ctypes.byref(pv)))
+
+    def set_colliders(self, k, colliders):
+        tris, ntris = _tri_array(colliders)
+        tp = tris.ctypes.data_as(_P(capi.Triangle)) if tris is not None else None
+        capi.check(self.lib.fgb_batch_set_colliders(self._h, k, tp, ntris))
+
+    def step(self, steps=1):
+        capi.check(self.lib.fgb_batch_step(self._h, steps))
+
+    def sync(self):
+        capi.check(self.lib.fgb_batch_sync(self._h))
+
+    def download(self, k):
+        n = self.counts[k]
+        out = {
+            "id": np.zeros(n, np.uint64),
+            "type": np.zeros(n, np.int32),
+            "mass": np.zeros(n, np.float32),
+            "position": np.zeros(3 * n, np.float32),
+            "velocity": np.zeros(3 * n, np.float32),
+            "colour": np.zeros(n, np.uint32),
+        }
+        pv = capi.particles_view(out)
+        capi.check(self.lib.fgb_batch_download(self._h, k, ctypes.byref(pv)))
+        return out
+
+    def surface(self, k):
+        mesh = capi.Mesh()
+        try:
+            capi.check(self.lib.fgb_batch_surface(self._h, k, ctypes.byref(mesh)))
+            return capi.mesh_to_numpy(mesh)
+        finally:
+            self.lib.fgb_mesh_free(ctypes.byref(mesh))
+
+    def surface_all(self):
+        counts = (ctypes.c_uint64 * self.n_scenes)()
+        capi.check(self.lib.fgb_batch_surface_all(self._h, counts))
+        return [int(c) for c in counts]
+
+    def surface_fetch(self, k):
+        mesh = capi.Mesh()
+        try:
+            capi.check(self.lib.fgb_batch_surface_fetch(self._h, k, ctypes.byref(mesh)))
+            return capi.mesh_to_numpy(mesh)
+        finally:
+            self.lib.fgb_mesh_free(ctypes.byref(mesh))
+
+    def probe(self, what, dtype):
+        nbytes = ctypes.c_uint64()
+        capi.check(self.lib.fgb_batch_probe_size(self._h, what, ctypes.byref(nbytes)))
+        out = np.zeros(int(nbytes.value) // np.dtype(dtype).itemsize, dtype)
+        capi.check(self.lib.fgb_batch_probe(self._h, what, out.ctypes.data_as(ctypes.c_void_p), nbytes.value))
+        return out
+
+    def grid_info(self, k):
+        gi = capi.GridInfo()
+        capi.check(self.lib.fgb_batch_grid_info(self._h, k, ctypes.byref(gi)))
+        return gi
+
+    def error_flags(self):
+        f = ctypes.c_uint32()
+        capi.check(self.lib.fgb_batch_error_flags(self._h, ctypes.byref(f)))
+        return int(f.value)
+
+    @property
+    def launches(self):
+        return int(self.lib.fgb_batch_launch_count(self._h))
+
+    def close(self):
+        if self._h:
+            self.lib.fgb_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
