@@ -1,0 +1,334 @@
+#!/usr/bin/env python
+"""Benchmark: PBF particle-steps/s (4 solver iterations) on one GB300.
+
+Default workload: dam_break_1m -- 1 048 576 particles (128x64x128 block, spacing
+0.05, seeded jitter) in [0,12.8]x[0,6.4]^2 with a static sphere r=1 at
+(8,0.8,3.2); h=0.1, rho0=1000, mass 0.125, dt=1/120, 4 iterations, s_corr, XSPH,
+vorticity; FP32.  A "step" is one PBF step of the whole scene.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value      whole-job particle-steps/s, state resident in HBM, L2 flushed (a
+           256 MiB write) before every timed step, each step timed with CUDA
+           events on the launching stream, max over ranks.
+e2e        the same metric through fgb_advance (the reference-facing C ABI call)
+           with host arrays: upload, step and write-back every step.
+roofline   the dominant kernel's algorithmic bytes per launch over its mean
+           CUDA-event duration, against the measured HBM copy bandwidth.
+cpu_baseline  the CPU oracle (a restatement of the reference's PBF path, OpenMP,
+           every host core) on a bounded sample of the same workload.
+Multi-GPU: one single-scene replica per rank (the step does not shard without a
+halo exchange), so scaling is weak.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PBF particle-steps/s (4 iters), batched vs per-scene; serving p50/p99 ms"
+UNIT = "particle-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+# Algorithmic (compulsory) bytes per particle of each kernel: every SoA array a
+# kernel must touch, once; neighbour re-reads are assumed to hit in cache.
+ALGO_BYTES = {
+    "predict": 44,      # x, v (32) + previous key (4) -> key, index (8)
+    "reorder": 112,     # key, index (8) + gather x, v, type, colour, slot (44) -> x, v, p*, type, colour, slot (60)
+    "lambda": 24,       # p* (16) -> lambda, density (8)
+    "delta": 36,        # p*, lambda (20) -> p* (16)
+    "vorticity": 64,    # p*, v (32) -> omega, XSPH velocity (32)
+    "vorticity_apply": 80,  # p*, omega, XSPH velocity (48) -> v, x (32)
+}
+
+
+def stage_names(iterations, baseline=True):
+    names = ["predict", "sort", "reorder"]
+    for _ in range(iterations):
+        names += ["lambda", "delta"]
+    if baseline:
+        names += ["vorticity", "vorticity_apply"]
+    return names
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{workload}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(seconds, params, make_scene):
+    """Time the CPU oracle (all host threads) on the workload until ~`seconds` pass."""
+    from oracle import oracle
+    oracle.build()
+    parts, cfg = make_scene()
+    n = len(parts["mass"])
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.step(params, cfg, parts)
+        steps += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"dam_break_1m ({n} particles), the first {steps} steps from the initial state, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from libfluid_gb300 import capi, scenes
+    from oracle import oracle
+    oracle.build()
+    params = capi.default_params(capi.PROFILE_BASELINE, 0.1)
+    parts, cfg = scenes.dam_break_1m()
+    n = len(parts["mass"])
+    for _ in range(args.warmup):
+        oracle.step(params, cfg, parts)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle.step(params, cfg, parts)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = n * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "dam_break_1m", "particles": n, "iterations": 4, "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"dam_break_1m, full steps {args.warmup + 1}..{args.warmup + args.steps}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own PBF cannot be built here (OpenCL path needs OpenCL; OpenMP path needs "
+                "GLM and does not compile); this arm times the CPU oracle, a restatement of that path",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from libfluid_gb300 import build, capi, scenes
+    from libfluid_gb300.solver import Batch, SphSolver
+    build.build()
+    params = capi.params(capi.PROFILE_BASELINE, 0.1)
+    parts, cfg = scenes.dam_break_1m()
+    n = len(parts["mass"])
+    solver = SphSolver(params=params)
+    stream = torch.cuda.current_stream()
+    solver.set_stream(stream.cuda_stream)
+    batch = Batch(solver, [(parts, cfg)])
+    batch.set_timing(True)
+    for _ in range(args.warmup):
+        batch.step(1)
+    batch.sync()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    names = stage_names(cfg.iterations)
+    stage_sum = [0.0] * len(names)
+    clocks = Clocks(local)
+    launches0 = batch.launches
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms = []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        flush.zero_()
+        ev0.record(stream)
+        batch.step(1)
+        ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        st = batch.stage_times()
+        for i, t in enumerate(st[:len(names)]):
+            stage_sum[i] += t
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = batch.launches - launches0
+    flags = batch.error_flags()
+    total_s = sum(step_ms) / 1e3
+    t = torch.tensor([total_s], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_s = float(t.item())
+    value = n * args.steps * world / max_s
+
+    # roofline of the dominant kernel
+    per_kernel = {}
+    for nm, tot in zip(names, stage_sum):
+        k = per_kernel.setdefault(nm, [0.0, 0])
+        k[0] += tot
+        k[1] += 1
+    gathers = {k: v for k, v in per_kernel.items() if k in ALGO_BYTES}
+    dom = max(gathers, key=lambda k: gathers[k][0])
+    launches_dom = gathers[dom][1] * args.steps
+    mean_ms = gathers[dom][0] / launches_dom
+    algo = ALGO_BYTES[dom] * n
+    achieved = algo / (mean_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic(dom, "dam_break_1m")
+    step_total = sum(stage_sum) / args.steps
+
+    # end to end through the reference-facing call with host buffers
+    e2e_steps = max(3, min(args.steps, 10))
+    host = scenes.copy_particles(parts)
+    e2e_solver = SphSolver(params=params)
+    for _ in range(2):
+        e2e_solver.advance(cfg, host)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_solver.advance(cfg, host)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = n * e2e_steps * world / float(te.item())
+    e2e_solver.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(args.cpu_seconds, params, scenes.dam_break_1m)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": max_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "dam_break_1m", "particles": n, "iterations": int(cfg.iterations),
+                       "sphere_collider": True, "l2": "flushed (256 MiB write) before every timed step",
+                       "parallelism": f"replicas x{world}", "cuda_graph": True},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 44 * n,
+                    "steps": e2e_steps, "call": "fgb_advance"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": algo,
+                         "mean_launch_ms": mean_ms},
+            "stages_ms_per_step": {nm: round(v[0] / args.steps, 4) for nm, v in per_kernel.items()},
+            "stage_sum_ms_per_step": step_total,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+            "error_flags": flags,
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+    solver.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

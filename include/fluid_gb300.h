@@ -171,6 +171,12 @@ int fgb_batch_sync(fgb_batch *b);
 int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags);
 /* Number of kernels this batch launched since creation (for accounting). */
 uint64_t fgb_batch_launch_count(const fgb_batch *b);
+/* Stage timing (replaces the reference's DEBUG-only clutil::Stopwatch phases,
+ * oclsph.hpp:666-934): when on, every step records CUDA events between its stages
+ * (predict, sort, reorder, lambda/delta per iteration, vorticity, vorticity apply);
+ * fgb_batch_stage_times returns the last step's per-stage milliseconds. */
+int fgb_batch_set_timing(fgb_batch *b, int on);
+int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count);
 
 /* Parity probes: copy an internal array of the last step to host memory.
  * what: FGB_PROBE_* ; bytes must equal the array size. */

@@ -183,6 +183,8 @@ _SIGS = {
     "fgb_batch_sync": (ctypes.c_int, [c_void_p]),
     "fgb_batch_error_flags": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),
+    "fgb_batch_set_timing": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "fgb_batch_stage_times": (ctypes.c_int, [c_void_p, P(ctypes.c_float), ctypes.c_uint32, P(ctypes.c_uint32)]),
     "fgb_batch_probe_size": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(ctypes.c_uint64)]),
     "fgb_batch_probe": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, ctypes.c_uint64]),
     "fgb_batch_grid_info": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(GridInfo)]),

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <functional>
 #include <cuda_runtime.h>
 
 #include "../../include/fluid_gb300.h"
@@ -57,7 +58,9 @@ void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, cudaStream_t st);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool last, cudaStream_t st);
-void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st);
+// `between` runs after the first of the two kernels (stage timing hook)
+void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
+                           const std::function<void()> &between = nullptr);
 // keys of the current positions (marching-cubes grid); ps_a receives solver-unit
 // positions in sorted order, cells the table
 void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st);

@@ -541,9 +541,10 @@ void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool l
             s.v1, last ? 1 : 0);
 }
 
-void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st) {
+void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {
     k_vorticity_xsph<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
                                                                   s.cells, ps, s.v1, s.type1, s.omega, s.vx);
+    if (between) between();
     k_vorticity_apply<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
                                                                    s.cells, ps, s.omega, s.vx, s.type1, s.v1, s.x1);
 }

@@ -255,6 +255,7 @@ struct fgb_batch {
     ~fgb_batch() {
         for (auto &g : graph)
             if (g) cudaGraphExecDestroy(g);
+        for (auto &ev : events) cudaEventDestroy(ev);
     }
 
     cudaStream_t stream() const { return solver->stream; }
@@ -295,32 +296,67 @@ struct fgb_batch {
         return s;
     }
 
+    // Stage timing: CUDA events recorded between the stages of a step (inside the
+    // captured graphs as external event nodes).  Stage order: predict, sort,
+    // reorder, then lambda/delta per iteration, then the two vorticity passes.
+    bool timing = false;
+    std::vector<cudaEvent_t> events;
+    uint32_t n_stages = 0;
+
+    void mark(uint32_t &k, cudaStream_t st) {
+        if (!timing) return;
+        if (k < events.size()) cudaEventRecordWithFlags(events[k], st, cudaEventRecordExternal);
+        ++k;
+    }
+
     // Enqueue one step that reads state set c and leaves the state in set c^1.
     int record_step(int c) {
         cudaStream_t st = stream();
         StepView s = view(c);
         uint64_t l = 0;
+        uint32_t k = 0;
+        mark(k, st);
         launch_predict_keys(s, st);
         l += 1;
+        mark(k, st);
         cudaError_t e = radix_sort_pairs(keys_in.p, vals_in.p, keys_sorted.p, vals_sorted.p, n, key_bits,
                                          sort_scratch.p, sort_scratch_bytes, st, err.p, &l);
         if (e != cudaSuccess) return fail_cuda(e, "step: radix sort");
+        mark(k, st);
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
         launch_reorder_cells(s, st);
         l += 1;
+        mark(k, st);
         for (uint32_t it = 0; it < iterations; ++it) {
             const float4 *pin = ps[it & 1].p;
             float4 *pout = ps[(it + 1) & 1].p;
             launch_lambda(s, pin, st);
+            mark(k, st);
             launch_delta(s, pin, pout, it + 1 == iterations, st);
+            mark(k, st);
             l += 2;
         }
         if (ph.profile != FGB_PROFILE_REF) {
-            launch_velocity_terms(s, ps[iterations & 1].p, st);
+            launch_velocity_terms(s, ps[iterations & 1].p, st, [&] { mark(k, st); });
+            mark(k, st);
             l += 2;
         }
         FGB_CUDA(cudaGetLastError(), "step: launch");
         launches_per_step = l;
+        if (timing) n_stages = k ? k - 1 : 0;
+        return FGB_OK;
+    }
+
+    int set_timing(bool on) {
+        if (on == timing) return FGB_OK;
+        timing = on;
+        if (on && events.empty()) {
+            events.resize(3 + 2 * iterations + 2 + 1);
+            for (auto &ev : events) FGB_CUDA(cudaEventCreate(&ev), "timing events");
+        }
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        graphs_ok = false;
         return FGB_OK;
     }
 
@@ -922,6 +958,21 @@ int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
 }
 
 uint64_t fgb_batch_launch_count(const fgb_batch *b) { return b ? b->launches : 0; }
+
+int fgb_batch_set_timing(fgb_batch *b, int on) {
+    if (!b) return fail(FGB_ERR_INVALID, "set_timing: null batch");
+    return b->set_timing(on != 0);
+}
+
+int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count) {
+    if (!b || !count) return fail(FGB_ERR_INVALID, "stage_times: bad argument");
+    if (!b->timing || b->n_stages == 0) return fail(FGB_ERR_INVALID, "stage_times: timing is off or no step ran");
+    FGB_CUDA(cudaStreamSynchronize(b->stream()), "stage_times: sync");
+    *count = b->n_stages;
+    for (uint32_t i = 0; i < b->n_stages && i < max; ++i)
+        FGB_CUDA(cudaEventElapsedTime(&ms[i], b->events[i], b->events[i + 1]), "stage_times");
+    return FGB_OK;
+}
 
 int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes) {
     if (!b || !bytes) return fail(FGB_ERR_INVALID, "probe: bad argument");

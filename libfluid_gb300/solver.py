@@ -151,6 +151,17 @@ class Batch:
         capi.check(self.lib.fgb_batch_error_flags(self._h, ctypes.byref(f)))
         return int(f.value)
 
+    def set_timing(self, on=True):
+        capi.check(self.lib.fgb_batch_set_timing(self._h, 1 if on else 0))
+
+    def stage_times(self):
+        """Per-stage milliseconds of the last step: predict, sort, reorder,
+        (lambda, delta) per iteration, then vorticity and vorticity apply."""
+        buf = (ctypes.c_float * 64)()
+        cnt = ctypes.c_uint32()
+        capi.check(self.lib.fgb_batch_stage_times(self._h, buf, 64, ctypes.byref(cnt)))
+        return [float(buf[i]) for i in range(cnt.value)]
+
     @property
     def launches(self):
         return int(self.lib.fgb_batch_launch_count(self._h))
