@@ -205,7 +205,10 @@ def run_ours(args):
     parts, cfg = scenes.dam_break_1m()
     n = len(parts["mass"])
     solver = SphSolver(params=params)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-legacy) stream: the library launches its graphs on it and the
+    # CUDA events below are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     solver.set_stream(stream.cuda_stream)
     batch = Batch(solver, [(parts, cfg)])
     batch.set_timing(True)

@@ -34,6 +34,9 @@ PROBE_LAMBDA = 4
 PROBE_DENSITY = 5
 PROBE_LATTICE = 6
 PROBE_CUBE_CASES = 7
+PROBE_LIST_COUNT = 8
+PROBE_LIST_VALID = 9
+PROBE_DISPLACEMENT = 10
 
 f3 = ctypes.c_float * 3
 

@@ -52,12 +52,25 @@ struct StepView {
     float4 *omega, *vx;
     uint32_t *err;
     int block;             // threads per CTA of the gather kernels
+    // per-step neighbour lists (Verlet lists with a skin), slot-major: list[j * n + a]
+    uint32_t *nlist;       // cap * n candidate indices, in 27-cell walk order
+    uint16_t *ncount;      // entries per particle (kListOverflow: walk the cells)
+    uint32_t cap;          // list capacity per particle (0: lists disabled)
+    float list_r2;         // (h + skin)^2: candidates kept at build time
+    float skin;            // a list stays exact while disp_a + max disp_b <= skin
+    float4 *ps_grid;       // p* at grid build (displacements are measured from it)
+    float *disp;           // |p - p_grid| per particle after the last delta pass
+    uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
+    uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
 };
+
+constexpr uint16_t kListOverflow = 0xffffu;
 
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
-void launch_lambda(const StepView &s, const float4 *ps, cudaStream_t st);
-void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool last, cudaStream_t st);
+void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
+void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
+                  cudaStream_t st);
 // `between` runs after the first of the two kernels (stage timing hook)
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
                            const std::function<void()> &between = nullptr);

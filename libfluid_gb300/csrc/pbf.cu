@@ -120,27 +120,162 @@ __global__ void k_reorder_cells(const SceneDev *__restrict__ scenes, const WellD
     }
 }
 
-template <int PROFILE>
-__global__ void __launch_bounds__(256) k_lambda(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n,
-                                                uint32_t mbits, const uint32_t *__restrict__ keys,
-                                                const uint2 *__restrict__ cells, const float4 *__restrict__ ps,
-                                                const int32_t *__restrict__ type, float *__restrict__ lambda,
-                                                float *__restrict__ density) {
+
+// ---------------------------------------------------------------- gathers
+//
+// Neighbour lists.  The reference walks the 27 cells of the grid built from p* at
+// the start of the step on every pass (oclsph_kernel.h:150-192); only ~16% of the
+// ~216 candidates lie within h.  The first lambda pass does that walk and also keeps,
+// per particle and in walk order, every candidate within h + skin (a Verlet list).
+// Later passes iterate the list instead of the cells.  A list is exact -- it holds
+// every candidate that the walk would find within h, in the walk's order -- while
+// disp_a + disp_b <= skin for all candidates b, where disp is the distance moved
+// since the grid was built: r_now <= h implies r_build <= h + disp_a + disp_b.  Each
+// delta pass records disp_a and a per-cell maximum; a particle whose bound fails (or
+// whose list overflowed) walks the cells.  Either way the per-particle sums see the
+// same candidates in the same order, so results are identical to the walk.
+
+struct GatherArgs {
+    const SceneDev *scenes;
+    const TriDev *tris;
+    Phys ph;
+    uint32_t n, mbits;
+    const uint32_t *keys;
+    const uint2 *cells;
+    const int32_t *type;
+    uint32_t *nlist;
+    uint16_t *ncount;
+    uint32_t cap;
+    float list_r2, skin;
+    const float4 *ps_grid;
+    float *disp;
+    uint32_t *cellmax;
+    uint8_t *valid;
+};
+
+enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
+
+__device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t *__restrict__ cellmax,
+                                               uint32_t key, uint32_t mbits) {
+    const uint32_t m = morton_of(key, mbits);
+    const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
+    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+    const uint32_t *tbl = cellmax + S.table_base;
+    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+    uint32_t best = 0;  // non-negative floats order like their bit patterns
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z > ez) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = cy + dy;
+            if (y < 0 || y > ey) continue;
+            const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
+            for (int x = x0; x <= x1; ++x) best = max(best, __ldg(&tbl[spread10((uint32_t)x) | yz]));
+        }
+    }
+    return __uint_as_float(best);
+}
+
+// Whether particle a may use its list for the current positions.
+template <int MODE>
+__device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key) {
+    if (A.cap == 0 || MODE == kBuild) return false;
+    const uint16_t c = A.ncount[a];
+    if (c == kListOverflow) return false;
+    if (MODE == kFresh) return true;
+    if (MODE == kStored) return A.valid[a] != 0;
+    const bool ok = A.disp[a] + max_cell_disp(S, A.cellmax, key, A.mbits) <= A.skin;
+    A.valid[a] = ok ? 1 : 0;
+    return ok;
+}
+
+// Visit the candidates of particle a in walk order as f(b, p_b).  Loads run four
+// candidates ahead of the arithmetic (indices, then positions), so the dependent
+// index -> position -> math chain does not serialise on memory latency.
+constexpr int kPrefetch = 4;
+
+template <class F>
+__device__ __forceinline__ void visit_range(uint32_t lo, uint32_t hi, const float4 *__restrict__ ps, F &f) {
+    uint32_t b = lo;
+    for (; b + kPrefetch <= hi; b += kPrefetch) {
+        float4 p[kPrefetch];
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k) p[k] = __ldg(&ps[b + k]);
+#pragma unroll
+        for (int k = 0; k < kPrefetch; ++k) f(b + k, p[k]);
+    }
+    for (; b < hi; ++b) f(b, __ldg(&ps[b]));
+}
+
+template <class F>
+__device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
+                                               bool list, const float4 *__restrict__ ps, F &&f) {
+    if (list) {
+        const uint32_t c = A.ncount[a];
+        const uint32_t *L = A.nlist + a;
+        const size_t n = A.n;
+        uint32_t j = 0;
+        for (; j + kPrefetch <= c; j += kPrefetch) {
+            uint32_t b[kPrefetch];
+            float4 p[kPrefetch];
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) b[k] = __ldg(L + (size_t)(j + k) * n);
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) p[k] = __ldg(&ps[b[k]]);
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) f(b[k], p[k]);
+        }
+        for (; j < c; ++j) {
+            const uint32_t b = __ldg(L + (size_t)j * n);
+            f(b, __ldg(&ps[b]));
+        }
+    } else {
+        const uint32_t m = morton_of(key, A.mbits);
+        const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
+        const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+        const uint2 *tbl = A.cells + S.table_base;
+        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int z = cz + dz;
+            if (z < 0 || z > ez) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy + dy;
+                if (y < 0 || y > ey) continue;
+                const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
+                for (int x = x0; x <= x1; ++x) {
+                    const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
+                    visit_range(c.x, c.y, ps, f);
+                }
+            }
+        }
+    }
+}
+
+template <int PROFILE, int MODE>
+__global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
+                                                float *__restrict__ lambda, float *__restrict__ density) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    if (type[a] == FGB_TYPE_OBSTACLE) {
+    if (a >= A.n) return;
+    if (A.type[a] == FGB_TYPE_OBSTACLE) {
         lambda[a] = 0.f;
         density[a] = 0.f;
+        if (MODE == kBuild && A.cap) A.ncount[a] = 0;
         return;
     }
-    const uint32_t key = keys[a];
-    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const Phys &ph = A.ph;
+    const uint32_t key = A.keys[a];
+    const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
+    const bool list = use_list<MODE>(A, S, a, key);
+    uint32_t built = 0;
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
-    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
-        const float4 pb = __ldg(&ps[b]);
+    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
+        if (MODE == kBuild && A.cap && r2 <= A.list_r2) {
+            if (built < A.cap) A.nlist[(size_t)built * A.n + a] = b;
+            ++built;
+        }
         if (PROFILE == kRef) {
             const float r = sqrtf(r2);
             if (r <= ph.h) {
@@ -170,6 +305,7 @@ __global__ void __launch_bounds__(256) k_lambda(const SceneDev *__restrict__ sce
             }
         }
     });
+    if (MODE == kBuild && A.cap) A.ncount[a] = built > A.cap ? kListOverflow : (uint16_t)built;
     float dens, lam;
     if (PROFILE == kRef) {
         dens = rho;
@@ -256,25 +392,26 @@ __device__ __forceinline__ void collide_sphere(const SceneDev &S, float *pos) {
     }
 }
 
-template <int PROFILE>
+
+template <int PROFILE, int MODE>
 __global__ void __launch_bounds__(256)
-    k_delta(const SceneDev *__restrict__ scenes, const TriDev *__restrict__ tris, Phys ph, uint32_t n, uint32_t mbits,
-            const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells, const float4 *__restrict__ ps_in,
-            const float *__restrict__ lambda, const int32_t *__restrict__ type, float4 *__restrict__ ps_out,
-            float4 *__restrict__ x, float4 *__restrict__ v, int last) {
+    k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
+            float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
+    if (a >= A.n) return;
     const float4 pa = ps_in[a];
-    if (type[a] == FGB_TYPE_OBSTACLE) {
+    if (A.type[a] == FGB_TYPE_OBSTACLE) {
         ps_out[a] = pa;
+        if (A.cap) A.disp[a] = 0.f;
         return;
     }
-    const uint32_t key = keys[a];
-    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const Phys &ph = A.ph;
+    const uint32_t key = A.keys[a];
+    const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
+    const bool list = use_list<MODE>(A, S, a, key);
     const float la = lambda[a];
     float px = 0.f, py = 0.f, pz = 0.f;
-    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
-        const float4 pb = __ldg(&ps_in[b]);
+    for_candidates(A, S, a, key, list, ps_in, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
@@ -323,7 +460,7 @@ __global__ void __launch_bounds__(256)
     float4 va = v[a];
     float vel[3] = {va.x, va.y, va.z};
     if (S.tri_count) {
-        collide_triangles(tris, S.tri_first, S.tri_count, world, vel);
+        collide_triangles(A.tris, S.tri_first, S.tri_count, world, vel);
         v[a] = make_float4(vel[0], vel[1], vel[2], va.w);
     }
     float q[3];
@@ -334,6 +471,14 @@ __global__ void __launch_bounds__(256)
         q[d] = w / S.scale;
     }
     ps_out[a] = make_float4(q[0], q[1], q[2], pa.w);
+    if (A.cap) {
+        // distance moved since the grid was built, for the list bound of later passes
+        const float4 g = A.ps_grid[a];
+        const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
+        const float d = sqrtf(ex * ex + ey * ey + ez * ez);
+        A.disp[a] = d;
+        atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
+    }
     if (last) {
         const float4 xa = x[a];
         const float xo[3] = {xa.x, xa.y, xa.z};
@@ -359,27 +504,28 @@ __device__ __forceinline__ void cross3(const float *a, const float *b, float *o)
 }
 
 // Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
+
+// Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
 __global__ void __launch_bounds__(256)
-    k_vorticity_xsph(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
-                     const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
-                     const float4 *__restrict__ ps, const float4 *__restrict__ v, const int32_t *__restrict__ type,
+    k_vorticity_xsph(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ v,
                      float4 *__restrict__ omega, float4 *__restrict__ vx) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
+    if (a >= A.n) return;
     const float4 va4 = v[a];
-    if (type[a] == FGB_TYPE_OBSTACLE) {
+    if (A.type[a] == FGB_TYPE_OBSTACLE) {
         omega[a] = make_float4(0.f, 0.f, 0.f, 0.f);
         vx[a] = va4;
         return;
     }
-    const uint32_t key = keys[a];
-    const SceneDev &S = scenes[scene_of(key, mbits)];
+    const Phys &ph = A.ph;
+    const uint32_t key = A.keys[a];
+    const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
+    const bool list = use_list<kCheck>(A, S, a, key);
     const float va[3] = {va4.x, va4.y, va4.z};
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
-    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
-        if (__ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
-        const float4 pb = __ldg(&ps[b]);
+    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+        if (__ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
@@ -411,22 +557,20 @@ __global__ void __launch_bounds__(256)
 
 // Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
 __global__ void __launch_bounds__(256)
-    k_vorticity_apply(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
-                      const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
-                      const float4 *__restrict__ ps, const float4 *__restrict__ omega,
-                      const float4 *__restrict__ vx, const int32_t *__restrict__ type, float4 *__restrict__ v,
-                      float4 *__restrict__ x) {
+    k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
+                      const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
-    if (type[a] == FGB_TYPE_OBSTACLE) return;
-    const uint32_t key = keys[a];
-    const SceneDev &S = scenes[scene_of(key, mbits)];
+    if (a >= A.n) return;
+    if (A.type[a] == FGB_TYPE_OBSTACLE) return;
+    const Phys &ph = A.ph;
+    const uint32_t key = A.keys[a];
+    const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     const float4 oa = omega[a];
+    const bool list = use_list<kStored>(A, S, a, key);
     float e[3] = {0.f, 0.f, 0.f};
-    for_neighbours(S, cells, key, mbits, [&](uint32_t b) {
-        if (__ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
-        const float4 pb = __ldg(&ps[b]);
+    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+        if (__ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
@@ -507,6 +651,28 @@ inline unsigned stream_grid(uint32_t n) {
     return g ? g : 1;
 }
 
+GatherArgs gather_args(const StepView &s) {
+    GatherArgs A;
+    A.scenes = s.scenes;
+    A.tris = s.tris;
+    A.ph = s.ph;
+    A.n = s.n;
+    A.mbits = s.mbits;
+    A.keys = s.keys_sorted;
+    A.cells = s.cells;
+    A.type = s.type1;
+    A.nlist = s.nlist;
+    A.ncount = s.ncount;
+    A.cap = s.cap;
+    A.list_r2 = s.list_r2;
+    A.skin = s.skin;
+    A.ps_grid = s.ps_grid;
+    A.disp = s.disp;
+    A.cellmax = s.cellmax;
+    A.valid = s.valid;
+    return A;
+}
+
 }  // namespace
 
 void launch_predict_keys(const StepView &s, cudaStream_t st) {
@@ -517,36 +683,44 @@ void launch_predict_keys(const StepView &s, cudaStream_t st) {
 void launch_reorder_cells(const StepView &s, cudaStream_t st) {
     k_reorder_cells<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.wells, s.ph, s.n, s.mbits, s.keys_sorted,
                                                       s.vals_sorted, s.x0, s.v0, s.type0, s.col0, s.slot0, s.x1,
-                                                      s.v1, s.type1, s.col1, s.slot1, s.ps_a, s.cells, s.cells_n,
+                                                      s.v1, s.type1, s.col1, s.slot1, s.ps_grid, s.cells, s.cells_n,
                                                       s.err);
 }
 
-void launch_lambda(const StepView &s, const float4 *ps, cudaStream_t st) {
-    if (s.ph.profile == FGB_PROFILE_REF)
-        k_lambda<FGB_PROFILE_REF><<<grid_for(s.n, s.block), s.block, 0, st>>>(
-            s.scenes, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps, s.type1, s.lambda, s.density);
-    else
-        k_lambda<FGB_PROFILE_BASELINE><<<grid_for(s.n, s.block), s.block, 0, st>>>(
-            s.scenes, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps, s.type1, s.lambda, s.density);
+void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st) {
+    const GatherArgs A = gather_args(s);
+    const unsigned g = grid_for(s.n, s.block);
+    const bool ref = s.ph.profile == FGB_PROFILE_REF;
+    if (iteration == 0) {
+        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+    } else {
+        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+    }
 }
 
-void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, bool last, cudaStream_t st) {
-    if (s.ph.profile == FGB_PROFILE_REF)
-        k_delta<FGB_PROFILE_REF><<<grid_for(s.n, s.block), s.block, 0, st>>>(
-            s.scenes, s.tris, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps_in, s.lambda, s.type1, ps_out, s.x1,
-            s.v1, last ? 1 : 0);
-    else
-        k_delta<FGB_PROFILE_BASELINE><<<grid_for(s.n, s.block), s.block, 0, st>>>(
-            s.scenes, s.tris, s.ph, s.n, s.mbits, s.keys_sorted, s.cells, ps_in, s.lambda, s.type1, ps_out, s.x1,
-            s.v1, last ? 1 : 0);
+void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
+                  cudaStream_t st) {
+    const GatherArgs A = gather_args(s);
+    const unsigned g = grid_for(s.n, s.block);
+    const bool ref = s.ph.profile == FGB_PROFILE_REF;
+    const int l = last ? 1 : 0;
+    if (iteration == 0) {
+        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+    } else {
+        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+    }
 }
 
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {
-    k_vorticity_xsph<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
-                                                                  s.cells, ps, s.v1, s.type1, s.omega, s.vx);
+    const GatherArgs A = gather_args(s);
+    const unsigned g = grid_for(s.n, s.block);
+    k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
     if (between) between();
-    k_vorticity_apply<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.scenes, s.ph, s.n, s.mbits, s.keys_sorted,
-                                                                   s.cells, ps, s.omega, s.vx, s.type1, s.v1, s.x1);
+    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1);
 }
 
 void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st) {

@@ -222,6 +222,14 @@ struct fgb_batch {
     Dev<uint2> cells;
     uint64_t cells_n = 0;
     Dev<float4> ps[2];
+    Dev<float4> ps_grid;
+    Dev<uint32_t> nlist;
+    Dev<uint16_t> ncount;
+    Dev<float> disp;
+    Dev<uint32_t> cellmax;
+    Dev<uint8_t> valid;
+    uint32_t list_cap = 96;
+    float skin_frac = 0.2f;
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
     Dev<uint32_t> err;
@@ -293,6 +301,17 @@ struct fgb_batch {
         s.vx = vx.p;
         s.err = err.p;
         s.block = solver->block;
+        s.nlist = nlist.p;
+        s.ncount = ncount.p;
+        s.cap = nlist.p ? list_cap : 0;
+        const float skin = skin_frac * ph.h;
+        const float reach = (ph.h + skin) * 1.00001f;
+        s.list_r2 = reach * reach;
+        s.skin = skin;
+        s.ps_grid = ps_grid.p;
+        s.disp = disp.p;
+        s.cellmax = cellmax.p;
+        s.valid = valid.p;
         return s;
     }
 
@@ -324,20 +343,23 @@ struct fgb_batch {
         if (e != cudaSuccess) return fail_cuda(e, "step: radix sort");
         mark(k, st);
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
+        if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
         mark(k, st);
+        // p* of the grid stays in ps_grid; the iterations ping-pong between ps[0] and ps[1]
+        const float4 *pin = ps_grid.p;
         for (uint32_t it = 0; it < iterations; ++it) {
-            const float4 *pin = ps[it & 1].p;
-            float4 *pout = ps[(it + 1) & 1].p;
-            launch_lambda(s, pin, st);
+            float4 *pout = ps[it & 1].p;
+            launch_lambda(s, pin, (int)it, st);
             mark(k, st);
-            launch_delta(s, pin, pout, it + 1 == iterations, st);
+            launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
             l += 2;
+            pin = pout;
         }
         if (ph.profile != FGB_PROFILE_REF) {
-            launch_velocity_terms(s, ps[iterations & 1].p, st, [&] { mark(k, st); });
+            launch_velocity_terms(s, pin, st, [&] { mark(k, st); });
             mark(k, st);
             l += 2;
         }
@@ -604,6 +626,17 @@ static int batch_init(fgb_batch *b) {
     b->sort_scratch_bytes = radix_scratch_bytes(n);
     FGB_CUDA(b->sort_scratch.alloc(b->sort_scratch_bytes), "batch alloc");
     FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
+    FGB_CUDA(b->ps_grid.alloc(n), "batch alloc");
+    if (const char *e = getenv("FGB_LIST_CAP")) b->list_cap = (uint32_t)atoi(e);
+    if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
+    if (b->list_cap > 4096) b->list_cap = 4096;
+    if (b->list_cap) {
+        FGB_CUDA(b->nlist.alloc(n * b->list_cap), "batch alloc neighbour lists");
+        FGB_CUDA(b->ncount.alloc(n), "batch alloc");
+        FGB_CUDA(b->disp.alloc(n), "batch alloc");
+        FGB_CUDA(b->valid.alloc(n), "batch alloc");
+        FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
+    }
     FGB_CUDA(b->lambda.alloc(n), "batch alloc");
     FGB_CUDA(b->density.alloc(n), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
@@ -985,6 +1018,9 @@ int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes) {
     case FGB_PROBE_CELLS: *bytes = b->cells_n * 8; break;
     case FGB_PROBE_LATTICE: *bytes = b->lat_total * 16; break;
     case FGB_PROBE_CUBE_CASES: *bytes = b->cube_total; break;
+    case FGB_PROBE_LIST_COUNT: *bytes = n * 2; break;
+    case FGB_PROBE_LIST_VALID: *bytes = n; break;
+    case FGB_PROBE_DISPLACEMENT: *bytes = n * 4; break;
     default: return fail(FGB_ERR_INVALID, "probe: unknown array");
     }
     return FGB_OK;
@@ -1004,6 +1040,9 @@ int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes)
     case FGB_PROBE_CELLS: src = b->cells.p; break;
     case FGB_PROBE_LATTICE: src = b->lattice.p; break;
     case FGB_PROBE_CUBE_CASES: src = b->cases.p; break;
+    case FGB_PROBE_LIST_COUNT: src = b->ncount.p; break;
+    case FGB_PROBE_LIST_VALID: src = b->valid.p; break;
+    case FGB_PROBE_DISPLACEMENT: src = b->disp.p; break;
     }
     if (!src) return fail(FGB_ERR_INVALID, "probe: array not allocated yet");
     cudaStream_t st = b->stream();
