@@ -57,6 +57,7 @@ struct Phys {
     float corr_n;
     float corr_ref;   // ref: poly6(dq)
     float corr_wdq;   // baseline: (h^2 - dq^2)^3
+    float inv_corr_ref, inv_corr_wdq;
     float xsph_c, vort_eps, damping;
     float mc_size, mc_infl;
     int profile;      // FGB_PROFILE_*

@@ -119,6 +119,8 @@ Phys make_phys(const fgb_params &p) {
         const float tt = hh - dq * dq;
         ph.corr_ref = (dq <= h) ? f * (tt * tt * tt) : 0.f;
     }
+    ph.inv_corr_ref = ph.corr_ref != 0.f ? 1.f / ph.corr_ref : 0.f;
+    ph.inv_corr_wdq = ph.corr_wdq != 0.f ? 1.f / ph.corr_wdq : 0.f;
     ph.corr_k = p.profile == FGB_PROFILE_REF ? p.corr_k : p.corr_k * hh;
     ph.xsph_c = p.xsph_c;
     ph.vort_eps = p.vorticity_epsilon;
@@ -194,6 +196,7 @@ struct fgb_solver {
     uint64_t cached_n = 0;
     fgb_config cached_cfg{};
     std::vector<TriDev> cached_tris;
+    std::vector<fgb_batch *> batches;  // every live batch; destroyed with the solver
 };
 
 struct fgb_batch {
@@ -757,7 +760,37 @@ static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
     return FGB_OK;
 }
 
-static void destroy_batch(fgb_batch *b) { delete b; }
+// Live handles: destroy calls check membership so that a stale or repeated
+// destroy is an error instead of a double free.
+static std::mutex g_handles_mu;
+static std::vector<const void *> g_handles;
+
+static void handle_add(const void *p) {
+    std::lock_guard<std::mutex> lk(g_handles_mu);
+    g_handles.push_back(p);
+}
+static bool handle_live(const void *p) {
+    std::lock_guard<std::mutex> lk(g_handles_mu);
+    return std::find(g_handles.begin(), g_handles.end(), p) != g_handles.end();
+}
+static bool handle_forget(const void *p) {
+    std::lock_guard<std::mutex> lk(g_handles_mu);
+    auto it = std::find(g_handles.begin(), g_handles.end(), p);
+    if (it == g_handles.end()) return false;
+    g_handles.erase(it);
+    return true;
+}
+
+static void destroy_batch(fgb_batch *b) {
+    if (!b) return;
+    handle_forget(b);
+    if (b->solver) {
+        auto &v = b->solver->batches;
+        v.erase(std::remove(v.begin(), v.end(), b), v.end());
+        if (b->solver->cached == b) b->solver->cached = nullptr;
+    }
+    delete b;
+}
 
 extern "C" {
 
@@ -842,13 +875,16 @@ int fgb_create(const fgb_params *params, fgb_solver **out) {
     }
     s->stream = s->own;
     ensure_tables();
+    handle_add(s);
     *out = s;
     return FGB_OK;
 }
 
 int fgb_destroy(fgb_solver *s) {
     if (!s) return FGB_OK;
-    if (s->cached) destroy_batch(s->cached);
+    if (!handle_forget(s)) return fail(FGB_ERR_INVALID, "destroy: not a live solver (destroyed twice?)");
+    if (s->own) cudaStreamSynchronize(s->own);
+    while (!s->batches.empty()) destroy_batch(s->batches.back());
     if (s->own) {
         cudaStreamSynchronize(s->own);
         cudaStreamDestroy(s->own);
@@ -883,12 +919,15 @@ int fgb_batch_create(fgb_solver *s, uint32_t n_scenes, const uint64_t *counts, c
         delete b;
         return rc;
     }
+    s->batches.push_back(b);
+    handle_add(b);
     *out = b;
     return FGB_OK;
 }
 
 int fgb_batch_destroy(fgb_batch *b) {
     if (!b) return FGB_OK;
+    if (!handle_live(b)) return fail(FGB_ERR_INVALID, "batch_destroy: not a live batch (its solver was destroyed?)");
     cudaStreamSynchronize(b->stream());
     destroy_batch(b);
     return FGB_OK;

@@ -8,13 +8,23 @@ returned.  Errors raise `capi.FluidError` carrying the library's status code,
 as the reference throws.  There is no CPU fallback: a missing CUDA library or
 device raises.
 """
+import atexit
 import ctypes
+import weakref
 
 import numpy as np
 
 from . import capi
 
 _P = ctypes.POINTER
+_live_solvers = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    # release device objects before the CUDA runtime shuts down at process exit
+    for s in list(_live_solvers):
+        s.close()
 
 
 def _tri_array(colliders):
@@ -31,7 +41,9 @@ class SphSolver:
         self.lib = capi.load()
         self.params = params if params is not None else capi.params(profile, h)
         self._h = ctypes.c_void_p()
+        self._batches = weakref.WeakSet()
         capi.check(self.lib.fgb_create(ctypes.byref(self.params), ctypes.byref(self._h)))
+        _live_solvers.add(self)
 
     @property
     def handle(self):
@@ -58,6 +70,9 @@ class SphSolver:
 
     def close(self):
         if self._h:
+            # the library destroys the solver's batches with it
+            for b in list(self._batches):
+                b._h = ctypes.c_void_p()
             self.lib.fgb_destroy(self._h)
             self._h = ctypes.c_void_p()
 
@@ -81,6 +96,7 @@ class Batch:
         self.configs = [c for _, c in scenes]
         self._h = ctypes.c_void_p()
         capi.check(self.lib.fgb_batch_create(solver.handle, self.n_scenes, counts, cfgs, ctypes.byref(self._h)))
+        solver._batches.add(self)
         for k, (parts, _) in enumerate(scenes):
             self.upload(k, parts)
 
@@ -167,9 +183,10 @@ class Batch:
         return int(self.lib.fgb_batch_launch_count(self._h))
 
     def close(self):
-        if self._h:
+        # a closed solver has already destroyed its batches
+        if self._h and self.solver._h:
             self.lib.fgb_batch_destroy(self._h)
-            self._h = ctypes.c_void_p()
+        self._h = ctypes.c_void_p()
 
     def __del__(self):
         try:
