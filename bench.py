@@ -316,6 +316,23 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def ncu_case():
+    """Four plain steps of dam_break_1m: per step, predict, 2 + passes sort kernels,
+    reorder, 4 x (lambda, delta), 2 vorticity kernels."""
+    from libfluid_gb300 import build, capi, scenes
+    from libfluid_gb300.solver import Batch, SphSolver
+    build.build()
+    params = capi.params(capi.PROFILE_BASELINE, 0.1)
+    parts, cfg = scenes.dam_break_1m()
+    solver = SphSolver(params=params)
+    batch = Batch(solver, [(parts, cfg)])
+    batch.step(4)
+    batch.sync()
+    print("ncu case done, error flags", batch.error_flags())
+    batch.close()
+    solver.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -324,7 +341,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="run 4 untimed steps of the workload and exit (the case that ncu captures)")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case()
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
