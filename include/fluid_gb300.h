@@ -220,6 +220,22 @@ uint64_t fgb_scan_scratch_bytes(uint64_t n);
 int fgb_exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
                            void *d_scratch, uint64_t scratch_bytes, void *cuda_stream);
 
+/* The same scan for callers that cannot allocate device memory (a host whose
+ * memory manager owns every device allocation, a plugin host that forbids its
+ * plugins to allocate, or a real-time loop where an allocation could block or
+ * fail).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its scratch is a fixed
+ * device array inside this library (about 33 KB, held by every GPU that loads the
+ * library until exit), so n must not exceed FGB_SCAN_NOALLOC_MAX_N (larger n
+ * returns FGB_ERR_CAPACITY).  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller.  It has no counterpart in the
+ * reference, whose triangle-count reduction allocates a buffer per call. */
+#define FGB_SCAN_NOALLOC_MAX_N 16777216ull
+int fgb_exclusive_scan_u32_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
+                                   void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
