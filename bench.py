@@ -154,6 +154,120 @@ def cpu_sample(seconds, params, make_scene):
                       f"{dt:.1f} s"}
 
 
+def bench_batched(params, steps=20, mc_every=10):
+    """Workload 4: 64 mixed scenes in one batch vs the same scenes stepped one by one."""
+    import torch
+    from libfluid_gb300 import scenes
+    from libfluid_gb300.solver import Batch, SphSolver
+    specs = scenes.batched_64()
+    total = sum(len(p["mass"]) for p, _ in specs)
+    solver = SphSolver(params=params)
+    batch = Batch(solver, [(scenes.copy_particles(p), c) for p, c in specs])
+    batch.step(3)
+    batch.sync()
+    launches0 = batch.launches
+    t0 = time.perf_counter()
+    tris = 0
+    for s in range(1, steps + 1):
+        batch.step(1)
+        if s % mc_every == 0:
+            tris += sum(batch.surface_all())
+    batch.sync()
+    t_batched = time.perf_counter() - t0
+    launches = batch.launches - launches0
+    batch.close()
+    singles = [Batch(solver, [(scenes.copy_particles(p), c)]) for p, c in specs]
+    for b in singles:
+        b.step(3)
+    for b in singles:
+        b.sync()
+    t0 = time.perf_counter()
+    for s in range(1, steps + 1):
+        for b in singles:
+            b.step(1)
+        if s % mc_every == 0:
+            for b in singles:
+                b.surface(0)
+    for b in singles:
+        b.sync()
+    t_loop = time.perf_counter() - t0
+    for b in singles:
+        b.close()
+    solver.close()
+    torch.cuda.synchronize()
+    v_b = total * steps / t_batched
+    v_l = total * steps / t_loop
+    return {"workload": "batched_64", "scenes": len(specs), "particles": total, "steps": steps,
+            "surface_every": mc_every, "batched_particle_steps_per_s": v_b, "per_scene_loop_particle_steps_per_s": v_l,
+            "speedup": v_b / v_l, "batched_launches": launches, "triangles": tris}
+
+
+def bench_serving(params, requests=48, run_seconds=25.0, seed=5):
+    """Workload 5: saturation throughput, then a Poisson stream at 80% of it."""
+    import numpy as np
+    from libfluid_gb300 import scenes
+    from libfluid_gb300.serve import Server
+    from libfluid_gb300.solver import SphSolver
+    cache = {}
+
+    def scene_for(n):
+        if n not in cache:
+            cache[n] = scenes.cube_scene(n, 5000 + len(cache))
+        return cache[n]
+
+    stream = scenes.serving_stream(requests, 1.0, seed=seed)
+    work = [(n, st, mesh) for _, n, st, mesh, _ in stream]
+    mean_ps = float(np.mean([n * st for n, st, _ in work]))
+    solver = SphSolver(params=params)
+
+    def saturate(one_at_a_time):
+        sv = Server(solver, one_at_a_time=one_at_a_time)
+        tickets = []
+        for n, st, mesh in work:
+            p, c = scene_for(n)
+            tickets.append(sv.submit(c, p, st, mesh))
+        sv.drain(1200)
+        s = sv.stats()
+        for t in tickets:
+            sv.fetch(t)
+        sv.close()
+        return s.particle_steps / s.elapsed_seconds, s
+
+    sat, s_sat = saturate(False)
+    loop, _ = saturate(True)
+    rate = 0.8 * sat / mean_ps
+    arrivals = scenes.serving_stream(100000, rate, seed=seed + 1)
+    sv = Server(solver)
+    t0 = time.perf_counter()
+    tickets = []
+    for t_arr, n, st, mesh, _ in arrivals:
+        if t_arr > run_seconds:
+            break
+        delay = t_arr - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        p, c = scene_for(n)
+        tickets.append(sv.submit(c, p, st, mesh))
+    sv.drain(1200)
+    res = [sv.poll(t) for t in tickets]
+    lat = sv.step_latencies()
+    s = sv.stats()
+    for t in tickets:
+        sv.fetch(t)
+    sv.close()
+    solver.close()
+    req = np.array([r.t_done - r.t_submit for r in res if r.status == 2])
+    pct = lambda a, q: float(np.percentile(a, q)) * 1e3 if len(a) else None  # noqa: E731
+    return {"workload": "serving", "saturation_particle_steps_per_s": sat,
+            "one_at_a_time_particle_steps_per_s": loop, "batching_gain": sat / loop,
+            "offered_fraction_of_saturation": 0.8, "arrival_rate_per_s": rate, "requests": len(tickets),
+            "completed": int(s.completed), "particle_steps_per_s": s.particle_steps / s.elapsed_seconds,
+            "step_ms": {"p50": pct(lat, 50), "p95": pct(lat, 95), "p99": pct(lat, 99)},
+            "request_ms": {"p50": pct(req, 50), "p95": pct(req, 95), "p99": pct(req, 99)},
+            "p99_over_p50_step": (pct(lat, 99) / pct(lat, 50)) if len(lat) else None,
+            "rebuilds": int(s.rebuilds), "rebuild_s": s.rebuild_seconds, "saturation_rebuilds": int(s_sat.rebuilds)}
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -287,6 +401,10 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_seconds, params, scenes.dam_break_1m)
+    batched = serving = None
+    if world == 1 and not args.no_extra:
+        batched = bench_batched(params)
+        serving = bench_serving(params)
 
     if rank == 0:
         line = {
@@ -308,6 +426,8 @@ def run_ours(args):
             "clocks": clk,
             "gpu_launches": launches,
             "error_flags": flags,
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     batch.close()
@@ -341,6 +461,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving legs")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run 4 untimed steps of the workload and exit (the case that ncu captures)")
     args = ap.parse_args()

@@ -206,6 +206,59 @@ typedef struct fgb_grid_info {
     float lattice_step;       /* solver units */
 } fgb_grid_info;
 int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out);
+/* Copy resident scene src_scene of src into dst_scene of dst on the device (same
+ * particle count, same solver).  The particle order is kept, so the scene's later
+ * steps are bit-identical to what src would have computed. */
+int fgb_batch_copy_scene(fgb_batch *dst, uint32_t dst_scene, fgb_batch *src, uint32_t src_scene);
+/* Device bytes one scene of n particles occupies in a batch (with its surface
+ * buffers when want_mesh); used for admission against an HBM budget. */
+int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, int want_mesh, uint64_t *bytes);
+
+/* ---- serving: a resident request loop with continuous batching ---------- */
+/* A worker thread admits requests in arrival order while the sum of their device
+ * footprints (fgb_scene_footprint) stays within half the budget (a membership
+ * change briefly holds two batches), keeps admitted scenes resident, and advances
+ * all of them together, one batched step per tick.  Finished scenes optionally
+ * get a surface; their final state waits on the host for fgb_serve_fetch.  Every
+ * request of one server must use the same iteration count.  While a server runs,
+ * its solver must not be used for other calls. */
+#define FGB_SERVE_WAITING 0
+#define FGB_SERVE_ACTIVE  1
+#define FGB_SERVE_DONE    2 /* negative status: the FGB_ERR_* that failed the request */
+
+typedef struct fgb_serve_options {
+    uint64_t budget_bytes;   /* HBM budget (0: 150 GiB) */
+    uint32_t max_active;     /* most scenes in one batch (0: 256) */
+    uint32_t one_at_a_time;  /* 1: no batching, one scene at a time (the comparison loop) */
+} fgb_serve_options;
+
+typedef struct fgb_serve_result {
+    uint64_t ticket;
+    uint64_t n;
+    uint32_t steps;
+    int32_t status;          /* FGB_SERVE_* or -FGB_ERR_* */
+    uint64_t triangles;
+    double t_submit, t_admit, t_done;  /* seconds since the server started */
+} fgb_serve_result;
+
+typedef struct fgb_serve_stats {
+    uint64_t ticks, particle_steps, completed, rejected, failed, active, waiting;
+    uint64_t used_bytes, budget_bytes, rebuilds;
+    double busy_seconds, rebuild_seconds, elapsed_seconds;
+} fgb_serve_stats;
+
+int fgb_serve_create(fgb_solver *s, const fgb_serve_options *opt, fgb_server **out);
+/* Copies the particles; returns a ticket. */
+int fgb_serve_submit(fgb_server *sv, const fgb_config *cfg, const fgb_particles *xs, uint32_t steps,
+                     int want_mesh, uint64_t *ticket);
+int fgb_serve_poll(fgb_server *sv, uint64_t ticket, fgb_serve_result *out);
+/* Final particles (Morton order) and mesh of a finished request; releases it. */
+int fgb_serve_fetch(fgb_server *sv, uint64_t ticket, fgb_particles *xs, fgb_mesh *mesh);
+int fgb_serve_get_stats(fgb_server *sv, fgb_serve_stats *out);
+/* Wall time of every tick (one batched step), in seconds. */
+int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
+int fgb_serve_drain(fgb_server *sv, double timeout_seconds);
+int fgb_serve_destroy(fgb_server *sv);
 
 /* ---- device building blocks (device pointers, caller-provided scratch) --- */
 /* Stable LSD radix sort of (key, value) u32 pairs on the low key_bits bits. */

@@ -122,27 +122,29 @@ class GridInfo(ctypes.Structure):
     ]
 
 
-class ServeRequest(ctypes.Structure):
+SERVE_WAITING = 0
+SERVE_ACTIVE = 1
+SERVE_DONE = 2
+
+
+class ServeOptions(ctypes.Structure):
     _fields_ = [
-        ("id", ctypes.c_uint64),
-        ("n", ctypes.c_uint64),
-        ("steps", ctypes.c_uint32),
-        ("want_mesh", ctypes.c_uint32),
-        ("seed", ctypes.c_uint64),
+        ("budget_bytes", ctypes.c_uint64),
+        ("max_active", ctypes.c_uint32),
+        ("one_at_a_time", ctypes.c_uint32),
     ]
 
 
 class ServeResult(ctypes.Structure):
     _fields_ = [
-        ("id", ctypes.c_uint64),
+        ("ticket", ctypes.c_uint64),
         ("n", ctypes.c_uint64),
         ("steps", ctypes.c_uint32),
         ("status", ctypes.c_int32),
         ("triangles", ctypes.c_uint64),
-        ("t_arrival", ctypes.c_double),
+        ("t_submit", ctypes.c_double),
         ("t_admit", ctypes.c_double),
         ("t_done", ctypes.c_double),
-        ("checksum", ctypes.c_double),
     ]
 
 
@@ -152,11 +154,15 @@ class ServeStats(ctypes.Structure):
         ("particle_steps", ctypes.c_uint64),
         ("completed", ctypes.c_uint64),
         ("rejected", ctypes.c_uint64),
+        ("failed", ctypes.c_uint64),
         ("active", ctypes.c_uint64),
         ("waiting", ctypes.c_uint64),
-        ("footprint_bytes", ctypes.c_uint64),
+        ("used_bytes", ctypes.c_uint64),
         ("budget_bytes", ctypes.c_uint64),
+        ("rebuilds", ctypes.c_uint64),
         ("busy_seconds", ctypes.c_double),
+        ("rebuild_seconds", ctypes.c_double),
+        ("elapsed_seconds", ctypes.c_double),
     ]
 
 
@@ -191,6 +197,19 @@ _SIGS = {
     "fgb_batch_probe_size": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(ctypes.c_uint64)]),
     "fgb_batch_probe": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, ctypes.c_uint64]),
     "fgb_batch_grid_info": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(GridInfo)]),
+    "fgb_batch_copy_scene": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, ctypes.c_uint32]),
+    "fgb_scene_footprint": (ctypes.c_int, [c_void_p, P(Config), ctypes.c_uint64, ctypes.c_int, P(ctypes.c_uint64)]),
+    "fgb_serve_create": (ctypes.c_int, [c_void_p, P(ServeOptions), P(c_void_p)]),
+    "fgb_serve_submit": (ctypes.c_int, [c_void_p, P(Config), P(Particles), ctypes.c_uint32, ctypes.c_int,
+                                        P(ctypes.c_uint64)]),
+    "fgb_serve_poll": (ctypes.c_int, [c_void_p, ctypes.c_uint64, P(ServeResult)]),
+    "fgb_serve_fetch": (ctypes.c_int, [c_void_p, ctypes.c_uint64, P(Particles), P(Mesh)]),
+    "fgb_serve_get_stats": (ctypes.c_int, [c_void_p, P(ServeStats)]),
+    "fgb_serve_step_latencies": (ctypes.c_int, [c_void_p, P(ctypes.c_double), ctypes.c_uint64,
+                                                P(ctypes.c_uint64)]),
+    "fgb_serve_drain": (ctypes.c_int, [c_void_p, ctypes.c_double]),
+    "fgb_serve_destroy": (ctypes.c_int, [c_void_p]),
+    "fgb_exclusive_scan_u32_noalloc": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p]),
     "fgb_radix_sort_scratch_bytes": (ctypes.c_uint64, [ctypes.c_uint64]),
     "fgb_radix_sort_pairs_u32": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_uint64,
                                                 ctypes.c_uint32, c_void_p, ctypes.c_uint64, c_void_p]),

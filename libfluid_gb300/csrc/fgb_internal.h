@@ -14,6 +14,9 @@ namespace fgb {
 int fail(int code, const char *msg);
 int fail_cuda(cudaError_t e, const char *where);
 
+// Morton key bits of one scene's grid under a solver's h (runtime.cu).
+uint32_t scene_morton_bits(const fgb_solver *s, const fgb_config *cfg);
+
 // radix sort (sort.cu)
 uint64_t radix_scratch_bytes(uint64_t n);
 int radix_passes(uint32_t key_bits);
@@ -66,6 +69,7 @@ struct StepView {
 
 constexpr uint16_t kListOverflow = 0xffffu;
 
+void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t value, cudaStream_t st);
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);

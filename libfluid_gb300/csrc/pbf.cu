@@ -12,6 +12,7 @@
 // fastest, oclsph_kernel.h:155-183) and each cell's particles in sorted order, so
 // every per-particle sum has one fixed order.  The solve is Jacobi: k_delta reads
 // one p* buffer and writes the other (the reference updates p* in place, a race).
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -674,6 +675,19 @@ GatherArgs gather_args(const StepView &s) {
 }
 
 }  // namespace
+
+namespace {
+__global__ void k_fill_u32(uint32_t *__restrict__ p, uint64_t n, uint32_t value) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+}  // namespace
+
+void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t value, cudaStream_t st) {
+    if (!n) return;
+    unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256, 152u * 8u);
+    k_fill_u32<<<g, 256, 0, st>>>(p, n, value);
+}
 
 void launch_predict_keys(const StepView &s, cudaStream_t st) {
     k_predict_keys<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.wells, s.ph, s.n, s.mbits, s.keys_prev, s.x0, s.v0,

@@ -716,6 +716,62 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     return FGB_OK;
 }
 
+// Device-to-device copy of one resident scene into another batch (the serving loop
+// moves running scenes into a new batch when its membership changes).  The segment
+// keeps its particle order, so the scene's next steps are bit-identical to what the
+// old batch -- or the scene alone -- would compute.
+static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_t sk) {
+    if (dk >= dst->n_scenes || sk >= src->n_scenes) return fail(FGB_ERR_INVALID, "copy_scene: scene out of range");
+    if (dst->counts[dk] != src->counts[sk]) return fail(FGB_ERR_INVALID, "copy_scene: particle counts differ");
+    const uint64_t n = src->counts[sk], fd = dst->first[dk], fs = src->first[sk];
+    cudaStream_t st = dst->stream();
+    FGB_CUDA(cudaStreamSynchronize(src->stream()), "copy_scene sync");
+    const int cd = dst->cur, cs = src->cur;
+    if (n) {
+        FGB_CUDA(cudaMemcpyAsync(dst->x[cd].p + fd, src->x[cs].p + fs, n * sizeof(float4), cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        FGB_CUDA(cudaMemcpyAsync(dst->v[cd].p + fd, src->v[cs].p + fs, n * sizeof(float4), cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        FGB_CUDA(cudaMemcpyAsync(dst->type[cd].p + fd, src->type[cs].p + fs, n * sizeof(int32_t),
+                                 cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        FGB_CUDA(cudaMemcpyAsync(dst->col[cd].p + fd, src->col[cs].p + fs, n * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        FGB_CUDA(cudaMemcpyAsync(dst->slot[cd].p + fd, src->slot[cs].p + fs, n * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        launch_fill_u32(dst->keys_sorted.p + fd, n, dst->mbits >= 32 ? 0u : (dk << dst->mbits), st);
+    }
+    dst->ids[dk] = src->ids[sk];
+    if (dst->scene_tris[dk].size() != src->scene_tris[sk].size() ||
+        (!src->scene_tris[sk].empty() && memcmp(dst->scene_tris[dk].data(), src->scene_tris[sk].data(),
+                                                src->scene_tris[sk].size() * sizeof(TriDev)) != 0)) {
+        dst->scene_tris[dk] = src->scene_tris[sk];
+        dst->tris_dirty = true;
+    }
+    FGB_CUDA(cudaStreamSynchronize(st), "copy_scene sync");
+    return FGB_OK;
+}
+
+// Device bytes a batch allocates for one scene (admission control of the serving
+// loop): per-particle arrays, the scene's cell table, and the surface buffers when a
+// mesh is wanted (triangles estimated at one per 20 cubes).
+static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64_t n, bool mesh, uint32_t cap) {
+    SceneDev S{};
+    scene_geometry(p, c, S);
+    const uint64_t table = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
+    uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * cap + 2 + 4 + 1;
+    if (p.profile != FGB_PROFILE_REF) per_particle += 32;
+    uint64_t bytes = per_particle * n + 12 * table;
+    if (mesh && S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1) {
+        const uint64_t samples = (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];
+        const uint64_t cubes = (uint64_t)(S.lat[0] - 1) * (S.lat[1] - 1) * (S.lat[2] - 1);
+        bytes += 32 * n + 20 * samples + 5 * cubes + sizeof(fgb_mesh_triangle) * (cubes / 20);
+    }
+    return bytes;
+}
+
 static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
     if (k >= b->n_scenes) return fail(FGB_ERR_INVALID, "download: scene out of range");
     if (!xs || xs->n != b->counts[k]) return fail(FGB_ERR_INVALID, "download: particle count differs");
@@ -1087,6 +1143,28 @@ int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes)
     cudaStream_t st = b->stream();
     if (bytes) FGB_CUDA(cudaMemcpyAsync(host_out, src, bytes, cudaMemcpyDeviceToHost, st), "probe");
     FGB_CUDA(cudaStreamSynchronize(st), "probe");
+    return FGB_OK;
+}
+
+extern "C++" {
+uint32_t fgb::scene_morton_bits(const fgb_solver *s, const fgb_config *cfg) {
+    SceneDev S{};
+    scene_geometry(s->params, *cfg, S);
+    return 3 * bits_for(std::max(S.ext[0], std::max(S.ext[1], S.ext[2])));
+}
+}
+
+int fgb_batch_copy_scene(fgb_batch *dst, uint32_t dst_scene, fgb_batch *src, uint32_t src_scene) {
+    if (!dst || !src) return fail(FGB_ERR_INVALID, "copy_scene: null batch");
+    if (dst->solver != src->solver) return fail(FGB_ERR_INVALID, "copy_scene: batches of different solvers");
+    return batch_copy_scene(dst, dst_scene, src, src_scene);
+}
+
+int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, int want_mesh, uint64_t *bytes) {
+    if (!s || !cfg || !bytes) return fail(FGB_ERR_INVALID, "footprint: bad argument");
+    uint32_t cap = 96;
+    if (const char *e = getenv("FGB_LIST_CAP")) cap = (uint32_t)atoi(e);
+    *bytes = scene_footprint(s->params, *cfg, n, want_mesh != 0, cap);
     return FGB_OK;
 }
 

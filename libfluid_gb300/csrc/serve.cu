@@ -1,0 +1,401 @@
+// serve.cu -- resident serving loop with continuous batching.
+//
+// Requests (a scene, a step count, optionally a final surface) arrive at any time.
+// A worker thread admits waiting requests in arrival order while their device
+// footprint fits the HBM budget, keeps every admitted scene resident on the device,
+// and advances all active scenes together: one tick = one step of one batch, i.e.
+// one launch per stage for every scene (fgb_batch_step).  When scenes finish or are
+// admitted, the survivors are copied device-to-device into a new batch with the new
+// membership (fgb_batch_copy_scene keeps their particle order, so a scene's result
+// is bit-identical alone and in any mix).  Finished scenes optionally run marching
+// cubes, their final state is copied to the host, and their memory is released.
+//
+// Budget accounting: a membership change holds the old and the new batch at once,
+// so admission keeps the sum of active footprints within half the budget.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "fgb_internal.h"
+
+namespace {
+
+using fgb::fail;
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+uint32_t bits_of(uint32_t v) {
+    uint32_t b = 0;
+    while ((1u << b) <= v && b < 31) ++b;
+    return b;
+}
+
+struct Request {
+    uint64_t ticket = 0;
+    fgb_config cfg{};
+    uint32_t steps = 0, remaining = 0;
+    bool want_mesh = false;
+    uint64_t n = 0, footprint = 0;
+    uint32_t mbits = 0;
+    std::vector<uint64_t> id;
+    std::vector<int32_t> type;
+    std::vector<float> mass, pos, vel;
+    std::vector<uint32_t> col;
+    double t_submit = 0, t_admit = -1, t_done = -1;
+    int32_t status = FGB_SERVE_WAITING;
+    uint64_t triangles = 0;
+    fgb_mesh mesh{nullptr, 0, 0};
+
+    fgb_particles view() {
+        return fgb_particles{n, id.data(), type.data(), mass.data(), pos.data(), vel.data(), col.data()};
+    }
+    ~Request() { fgb_mesh_free(&mesh); }
+};
+
+}  // namespace
+
+struct fgb_server {
+    fgb_solver *solver = nullptr;
+    fgb_serve_options opt{};
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<Request *> waiting;                       // admitted in arrival order
+    std::vector<Request *> live;                         // admitted and still running
+    std::map<uint64_t, std::unique_ptr<Request>> requests;
+    uint64_t used = 0, next_ticket = 1;
+    bool stop = false;
+    double t0 = 0;
+    // worker-only state
+    fgb_batch *batch = nullptr;
+    std::vector<Request *> batch_scenes;  // scene k of `batch` is batch_scenes[k]
+    std::thread worker;
+    // statistics (under mu)
+    uint64_t ticks = 0, particle_steps = 0, completed = 0, rejected = 0, failed = 0, rebuilds = 0;
+    double busy = 0, rebuild_time = 0;
+    std::vector<double> step_latency;
+    std::string last_error;
+
+    double t() const { return now_s() - t0; }
+
+    // Admit waiting requests (mu held); returns the scenes of the next tick.
+    std::vector<Request *> admit() {
+        const uint64_t cap_bytes = opt.budget_bytes / 2;
+        uint32_t mbits = 0;
+        for (Request *r : live) mbits = std::max(mbits, r->mbits);
+        while (!waiting.empty()) {
+            Request *r = waiting.front();
+            if (r->footprint > cap_bytes) {  // could never fit
+                waiting.pop_front();
+                r->status = -FGB_ERR_BUDGET;
+                r->t_done = t();
+                rejected++;
+                continue;
+            }
+            if (opt.one_at_a_time && !live.empty()) break;
+            if (live.size() >= opt.max_active) break;
+            const uint32_t mb = std::max(mbits, r->mbits);
+            if (mb + bits_of((uint32_t)live.size()) > 32) break;  // scene id above the Morton key
+            if (used + r->footprint > cap_bytes) break;
+            waiting.pop_front();
+            used += r->footprint;
+            mbits = mb;
+            r->status = FGB_SERVE_ACTIVE;
+            r->t_admit = t();
+            live.push_back(r);
+        }
+        return live;
+    }
+
+    // Make `batch` hold exactly `next`; survivors move on the device.
+    int rebuild(const std::vector<Request *> &next) {
+        const double r0 = now_s();
+        fgb_batch *nb = nullptr;
+        if (!next.empty()) {
+            std::vector<uint64_t> counts;
+            std::vector<fgb_config> cfgs;
+            for (Request *r : next) {
+                counts.push_back(r->n);
+                cfgs.push_back(r->cfg);
+            }
+            int rc = fgb_batch_create(solver, (uint32_t)next.size(), counts.data(), cfgs.data(), &nb);
+            if (rc) return rc;
+            for (size_t k = 0; k < next.size(); ++k) {
+                Request *r = next[k];
+                auto it = std::find(batch_scenes.begin(), batch_scenes.end(), r);
+                if (it != batch_scenes.end()) {
+                    rc = fgb_batch_copy_scene(nb, (uint32_t)k, batch, (uint32_t)(it - batch_scenes.begin()));
+                } else {
+                    fgb_particles v = r->view();
+                    rc = fgb_batch_upload(nb, (uint32_t)k, &v);
+                }
+                if (rc) {
+                    fgb_batch_destroy(nb);
+                    return rc;
+                }
+            }
+        }
+        if (batch) fgb_batch_destroy(batch);
+        batch = nb;
+        batch_scenes = next;
+        std::lock_guard<std::mutex> lk(mu);
+        rebuilds++;
+        rebuild_time += now_s() - r0;
+        return FGB_OK;
+    }
+
+    void fail_scenes(const std::vector<Request *> &scenes, int rc) {
+        std::lock_guard<std::mutex> lk(mu);
+        last_error = fgb_last_error();
+        for (Request *r : scenes) {
+            if (r->status != FGB_SERVE_ACTIVE) continue;
+            r->status = -rc;
+            r->t_done = t();
+            used -= r->footprint;
+            failed++;
+        }
+        std::vector<Request *> keep;
+        for (Request *r : live)
+            if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
+        live.swap(keep);
+        cv.notify_all();
+    }
+
+    void run() {
+        cudaSetDevice(device);
+        for (;;) {
+            std::vector<Request *> next;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !waiting.empty() || !live.empty(); });
+                if (stop) break;
+                next = admit();
+            }
+            if (next != batch_scenes) {
+                int rc = rebuild(next);
+                if (rc) {
+                    if (batch) fgb_batch_destroy(batch);
+                    batch = nullptr;
+                    batch_scenes.clear();
+                    fail_scenes(next, rc);
+                    continue;
+                }
+            }
+            if (batch_scenes.empty()) continue;
+            uint64_t particles = 0;
+            for (Request *r : batch_scenes) particles += r->n;
+            const double s0 = now_s();
+            int rc = fgb_batch_step(batch, 1);
+            if (!rc) rc = fgb_batch_sync(batch);
+            const double s1 = now_s();
+            if (rc) {
+                fail_scenes(batch_scenes, rc);
+                fgb_batch_destroy(batch);
+                batch = nullptr;
+                batch_scenes.clear();
+                continue;
+            }
+            std::vector<Request *> done;
+            for (size_t k = 0; k < batch_scenes.size(); ++k) {
+                Request *r = batch_scenes[k];
+                if (--r->remaining) continue;
+                if (r->want_mesh) {
+                    rc = fgb_batch_surface(batch, (uint32_t)k, &r->mesh);
+                    if (rc) break;
+                    r->triangles = r->mesh.n;
+                }
+                fgb_particles v = r->view();
+                rc = fgb_batch_download(batch, (uint32_t)k, &v);
+                if (rc) break;
+                done.push_back(r);
+            }
+            if (rc) {
+                fail_scenes(batch_scenes, rc);
+                fgb_batch_destroy(batch);
+                batch = nullptr;
+                batch_scenes.clear();
+                continue;
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            step_latency.push_back(s1 - s0);
+            busy += s1 - s0;
+            ticks++;
+            particle_steps += particles;
+            for (Request *r : done) {
+                r->status = FGB_SERVE_DONE;
+                r->t_done = t();
+                used -= r->footprint;
+                completed++;
+            }
+            if (!done.empty()) {
+                std::vector<Request *> keep;
+                for (Request *r : live)
+                    if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
+                live.swap(keep);
+            }
+            cv.notify_all();
+        }
+        if (batch) fgb_batch_destroy(batch);
+        batch = nullptr;
+    }
+};
+
+extern "C" {
+
+int fgb_serve_create(fgb_solver *s, const fgb_serve_options *opt, fgb_server **out) {
+    if (!s || !out) return fail(FGB_ERR_INVALID, "serve_create: null argument");
+    fgb_server *sv = new fgb_server();
+    sv->solver = s;
+    if (opt) sv->opt = *opt;
+    if (!sv->opt.budget_bytes) sv->opt.budget_bytes = 150ull << 30;
+    if (!sv->opt.max_active) sv->opt.max_active = 256;
+    cudaGetDevice(&sv->device);
+    sv->t0 = now_s();
+    sv->worker = std::thread([sv] { sv->run(); });
+    *out = sv;
+    return FGB_OK;
+}
+
+int fgb_serve_submit(fgb_server *sv, const fgb_config *cfg, const fgb_particles *xs, uint32_t steps,
+                     int want_mesh, uint64_t *ticket) {
+    if (!sv || !cfg || !xs || !ticket) return fail(FGB_ERR_INVALID, "serve_submit: null argument");
+    if (steps == 0) return fail(FGB_ERR_INVALID, "serve_submit: steps must be >= 1");
+    if (xs->n == 0 || !xs->position || !xs->velocity || !xs->mass || !xs->type)
+        return fail(FGB_ERR_INVALID, "serve_submit: empty or incomplete particle arrays");
+    auto r = std::make_unique<Request>();
+    r->cfg = *cfg;
+    r->steps = r->remaining = steps;
+    r->want_mesh = want_mesh != 0;
+    r->n = xs->n;
+    int rc = fgb_scene_footprint(sv->solver, cfg, xs->n, want_mesh, &r->footprint);
+    if (rc) return rc;
+    // Morton bits of the scene's grid: admission keeps scene id + key within 32 bits
+    r->mbits = fgb::scene_morton_bits(sv->solver, cfg);
+    r->id.assign(xs->n, 0);
+    r->type.assign(xs->type, xs->type + xs->n);
+    r->mass.assign(xs->mass, xs->mass + xs->n);
+    r->pos.assign(xs->position, xs->position + 3 * xs->n);
+    r->vel.assign(xs->velocity, xs->velocity + 3 * xs->n);
+    r->col.assign(xs->n, 0xffffffffu);
+    for (uint64_t i = 0; i < xs->n; ++i) {
+        r->id[i] = xs->id ? xs->id[i] : i;
+        if (xs->colour) r->col[i] = xs->colour[i];
+    }
+    std::lock_guard<std::mutex> lk(sv->mu);
+    r->ticket = sv->next_ticket++;
+    r->t_submit = sv->t();
+    *ticket = r->ticket;
+    sv->waiting.push_back(r.get());
+    sv->requests[r->ticket] = std::move(r);
+    sv->cv.notify_all();
+    return FGB_OK;
+}
+
+int fgb_serve_poll(fgb_server *sv, uint64_t ticket, fgb_serve_result *out) {
+    if (!sv || !out) return fail(FGB_ERR_INVALID, "serve_poll: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->requests.find(ticket);
+    if (it == sv->requests.end()) return fail(FGB_ERR_INVALID, "serve_poll: unknown ticket");
+    const Request &r = *it->second;
+    out->ticket = r.ticket;
+    out->n = r.n;
+    out->steps = r.steps;
+    out->status = r.status;
+    out->triangles = r.triangles;
+    out->t_submit = r.t_submit;
+    out->t_admit = r.t_admit;
+    out->t_done = r.t_done;
+    return FGB_OK;
+}
+
+int fgb_serve_fetch(fgb_server *sv, uint64_t ticket, fgb_particles *xs, fgb_mesh *mesh) {
+    if (!sv) return fail(FGB_ERR_INVALID, "serve_fetch: null server");
+    std::unique_ptr<Request> r;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        auto it = sv->requests.find(ticket);
+        if (it == sv->requests.end()) return fail(FGB_ERR_INVALID, "serve_fetch: unknown ticket");
+        const int32_t st = it->second->status;
+        if (st == FGB_SERVE_WAITING || st == FGB_SERVE_ACTIVE) return fail(FGB_ERR_INVALID, "serve_fetch: not done");
+        r = std::move(it->second);
+        sv->requests.erase(it);
+    }
+    if (r->status != FGB_SERVE_DONE) return fail(-r->status, "serve_fetch: request failed or was rejected");
+    if (xs) {
+        if (xs->n != r->n) return fail(FGB_ERR_INVALID, "serve_fetch: particle count differs");
+        if (xs->id) memcpy(xs->id, r->id.data(), r->n * sizeof(uint64_t));
+        if (xs->type) memcpy(xs->type, r->type.data(), r->n * sizeof(int32_t));
+        if (xs->mass) memcpy(xs->mass, r->mass.data(), r->n * sizeof(float));
+        if (xs->position) memcpy(xs->position, r->pos.data(), 3 * r->n * sizeof(float));
+        if (xs->velocity) memcpy(xs->velocity, r->vel.data(), 3 * r->n * sizeof(float));
+        if (xs->colour) memcpy(xs->colour, r->col.data(), r->n * sizeof(uint32_t));
+    }
+    if (mesh) {
+        fgb_mesh_free(mesh);
+        *mesh = r->mesh;  // ownership moves to the caller
+        r->mesh = fgb_mesh{nullptr, 0, 0};
+    }
+    return FGB_OK;
+}
+
+int fgb_serve_get_stats(fgb_server *sv, fgb_serve_stats *out) {
+    if (!sv || !out) return fail(FGB_ERR_INVALID, "serve_stats: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    out->ticks = sv->ticks;
+    out->particle_steps = sv->particle_steps;
+    out->completed = sv->completed;
+    out->rejected = sv->rejected;
+    out->failed = sv->failed;
+    out->active = sv->live.size();
+    out->waiting = sv->waiting.size();
+    out->used_bytes = sv->used;
+    out->budget_bytes = sv->opt.budget_bytes;
+    out->rebuilds = sv->rebuilds;
+    out->busy_seconds = sv->busy;
+    out->rebuild_seconds = sv->rebuild_time;
+    out->elapsed_seconds = sv->t();
+    return FGB_OK;
+}
+
+int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t *count) {
+    if (!sv || !count) return fail(FGB_ERR_INVALID, "serve_step_latencies: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->step_latency.size();
+    for (uint64_t i = 0; out && i < max && i < sv->step_latency.size(); ++i) out[i] = sv->step_latency[i];
+    return FGB_OK;
+}
+
+int fgb_serve_drain(fgb_server *sv, double timeout_seconds) {
+    if (!sv) return fail(FGB_ERR_INVALID, "serve_drain: null server");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    const bool ok = sv->cv.wait_for(lk, std::chrono::duration<double>(timeout_seconds),
+                                    [&] { return sv->waiting.empty() && sv->live.empty(); });
+    if (!ok) return fail(FGB_ERR_TIMEOUT, "serve_drain: requests still pending at the timeout");
+    return FGB_OK;
+}
+
+int fgb_serve_destroy(fgb_server *sv) {
+    if (!sv) return FGB_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    delete sv;
+    return FGB_OK;
+}
+
+}  // extern "C"
+

@@ -109,10 +109,16 @@ def double_dam_8m(iterations=4):
     return concat([a, b]), config((0.0, 0.0, 0.0), (25.6, 12.8, 12.8), iterations=iterations)
 
 
+def cube_side(n_target):
+    """Cube side (particles) of the batched/serving recipe: the cube root of n rounded
+    to the nearest multiple of 8 (halves round up), at least 8."""
+    return max(8, int(math.floor(n_target ** (1.0 / 3.0) / 8.0 + 0.5)) * 8)
+
+
 def cube_scene(n_target, seed, iterations=4):
     """A scene of the batched/serving recipe: cube side = cbrt(n) rounded to a
     multiple of 8; box 2x the block extent in x, 1.5x in y and z."""
-    side = max(8, int(round(round(n_target ** (1.0 / 3.0)) / 8.0)) * 8)
+    side = cube_side(n_target)
     ext = side * SPACING
     parts = block((side, side, side), (0.0, 0.0, 0.0), seed)
     return parts, config((0.0, 0.0, 0.0), (2.0 * ext, 1.5 * ext, 1.5 * ext), iterations=iterations)
@@ -139,13 +145,13 @@ def serving_stream(count, rate_hz, seed=5, lo=16384, hi=2097152):
     mesh = (u[:, 3] < 0.5).astype(np.int64)
     out = []
     for i in range(count):
-        side = max(8, int(round(round(n[i] ** (1.0 / 3.0)) / 8.0)) * 8)
+        side = cube_side(n[i])
         out.append((float(t[i]), side ** 3, int(steps[i]), int(mesh[i]), 5 * 104729 + i))
     return out
 
 
 def realised_count(n_target):
-    side = max(8, int(round(round(n_target ** (1.0 / 3.0)) / 8.0)) * 8)
+    side = cube_side(n_target)
     return side ** 3
 
 

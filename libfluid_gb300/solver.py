@@ -42,6 +42,7 @@ class SphSolver:
         self.params = params if params is not None else capi.params(profile, h)
         self._h = ctypes.c_void_p()
         self._batches = weakref.WeakSet()
+        self._servers = weakref.WeakSet()
         capi.check(self.lib.fgb_create(ctypes.byref(self.params), ctypes.byref(self._h)))
         _live_solvers.add(self)
 
@@ -71,6 +72,8 @@ class SphSolver:
     def close(self):
         if self._h:
             # the library destroys the solver's batches with it
+            for sv in list(self._servers):  # a server's worker uses the solver
+                sv.close()
             for b in list(self._batches):
                 b._h = ctypes.c_void_p()
             self.lib.fgb_destroy(self._h)

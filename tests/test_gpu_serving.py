@@ -1,0 +1,87 @@
+"""Serving loop on the GPU: requests of different sizes and step counts arriving
+while others run are admitted, batched and finished; each result is identical to
+the same scene advanced alone, and to the one-at-a-time loop."""
+import time
+
+import numpy as np
+import pytest
+
+from libfluid_gb300 import capi, scenes
+from libfluid_gb300.serve import Server
+from libfluid_gb300.solver import Batch, SphSolver
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests():
+    out = []
+    for i, (n, steps, mesh) in enumerate([(9000, 7, True), (30000, 4, False), (12000, 9, True),
+                                           (5000, 3, False), (20000, 6, True)]):
+        parts, cfg = scenes.cube_scene(n, 700 + i)
+        out.append((parts, cfg, steps, mesh))
+    return out
+
+
+def _alone(solver, parts, cfg, steps, mesh):
+    b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+    b.step(steps)
+    got = b.download(0)
+    tris = b.surface(0) if mesh else None
+    b.close()
+    return got, tris
+
+
+def _serve(solver, reqs, one_at_a_time=False, stagger=0.0):
+    sv = Server(solver, budget_bytes=8 << 30, one_at_a_time=one_at_a_time)
+    tickets = []
+    for parts, cfg, steps, mesh in reqs:
+        tickets.append(sv.submit(cfg, parts, steps, mesh))
+        if stagger:
+            time.sleep(stagger)  # later requests arrive while earlier ones run
+    sv.drain(300)
+    results = [sv.fetch(t) for t in tickets]
+    st = sv.stats()
+    lat = sv.step_latencies()
+    sv.close()
+    return results, st, lat
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix():
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    reqs = _requests()
+    mixed, st, lat = _serve(solver, reqs, stagger=0.002)
+    assert st.completed == len(reqs) and st.failed == 0 and st.rejected == 0
+    assert st.ticks >= max(r[2] for r in reqs)
+    assert len(lat) == st.ticks
+    # continuous batching: fewer ticks than running the requests back to back
+    assert st.ticks < sum(r[2] for r in reqs)
+    for (parts, cfg, steps, mesh), (got, tris) in zip(reqs, mixed):
+        ref, rtris = _alone(solver, parts, cfg, steps, mesh)
+        for f in ("id", "position", "velocity", "colour"):
+            assert (got[f] == ref[f]).all(), f
+        if mesh:
+            assert len(tris) == len(rtris) and (tris == rtris).all()
+    serial, st1, _ = _serve(solver, reqs, one_at_a_time=True)
+    assert st1.ticks == sum(r[2] for r in reqs)
+    for (got, tris), (got1, tris1) in zip(mixed, serial):
+        assert (got["position"] == got1["position"]).all()
+    solver.close()
+
+
+def test_over_budget_request_is_rejected_and_others_complete():
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    big, cfg = scenes.cube_scene(262144, 1)
+    small, cfg2 = scenes.cube_scene(8000, 2)
+    sv = Server(solver, budget_bytes=64 << 20)  # 64 MiB: the big scene can never fit
+    t_big = sv.submit(cfg, big, 2)
+    t_small = sv.submit(cfg2, small, 2)
+    sv.drain(120)
+    assert sv.poll(t_big).status == -capi.FGB_ERR_BUDGET
+    assert sv.poll(t_small).status == capi.SERVE_DONE
+    got, _ = sv.fetch(t_small)
+    ref, _ = _alone(solver, small, cfg2, 2, False)
+    assert (got["position"] == ref["position"]).all()
+    with pytest.raises(capi.FluidError):
+        sv.fetch(t_big)
+    sv.close()
+    solver.close()
