@@ -17,7 +17,7 @@ def _compile(tmp_path):
     from libfluid_gb300 import build
     build.build()
     exe = str(tmp_path / "adapter_demo")
-    cmd = ["g++", "-std=c++14", "-O2", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), SRC,
+    cmd = ["g++", "-std=c++14", "-O2", "-ffp-contract=off", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"), SRC,
            "-L" + LIBDIR, "-lfluidgb", "-Wl,-rpath," + LIBDIR, "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -38,7 +38,9 @@ def test_adapter_matches_c_abi(tmp_path):
     from libfluid_gb300 import capi
     from libfluid_gb300.solver import SphSolver
     ix, iy, iz = np.meshgrid(np.arange(12), np.arange(12), np.arange(12), indexing="ij")
-    pos = np.stack([0.025 + 0.05 * ix.ravel(), 0.025 + 0.05 * iy.ravel(), 0.025 + 0.05 * iz.ravel()], 1)
+    # the same float32 operations as the C++ program: 0.025f + 0.05f * x
+    f = lambda a: np.float32(0.025) + np.float32(0.05) * a.ravel().astype(np.float32)  # noqa: E731
+    pos = np.stack([f(ix), f(iy), f(iz)], 1)
     n = len(pos)
     parts = {"id": np.arange(n, dtype=np.uint64), "type": np.zeros(n, np.int32), "mass": np.ones(n, np.float32),
              "position": pos.astype(np.float32).ravel(), "velocity": np.zeros(3 * n, np.float32),
