@@ -65,6 +65,12 @@ struct StepView {
     float *disp;           // |p - p_grid| per particle after the last delta pass
     uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
+    // per-pass hit lists: the candidates of one pass that lie within h (and not on top
+    // of the particle), in walk order; written by a lambda / vorticity pass, read by the
+    // delta / vorticity-apply pass over the same positions.  Slot-major like nlist.
+    uint32_t *hlist;       // hcap * n
+    uint16_t *hcount;      // entries per particle (kListOverflow: use nlist / the cells)
+    uint32_t hcap;
 };
 
 constexpr uint16_t kListOverflow = 0xffffu;

@@ -152,6 +152,9 @@ struct GatherArgs {
     float *disp;
     uint32_t *cellmax;
     uint8_t *valid;
+    uint32_t *hlist;
+    uint16_t *hcount;
+    uint32_t hcap;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -252,6 +255,70 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
     }
 }
 
+// Hit lists.  A lambda pass and the delta pass after it read the same p*, so they
+// agree on which candidates lie within h; likewise the two vorticity passes.  The
+// first pass of each pair appends those candidates (in walk order) to a per-pass hit
+// list, and the second iterates it: about 35 entries instead of the ~60 of the Verlet
+// list or the ~216 of the cell walk, with no lanes idling on the range test.  The
+// second pass still applies its own range tests to each hit, so its sums are
+// bit-identical to a walk.  Rows are particle-major (hcap entries, hcap a multiple of
+// 4) and move as 16-byte vectors: four hits per store and per load.
+struct HitWriter {
+    uint4 *row;
+    uint32_t cap, count = 0;
+    uint4 q;
+    __device__ __forceinline__ HitWriter(const GatherArgs &A, uint32_t a)
+        : row(reinterpret_cast<uint4 *>(A.hlist + (size_t)a * A.hcap)), cap(A.hcap) {}
+    __device__ __forceinline__ void add(uint32_t b) {
+        const uint32_t k = count & 3u;
+        q.x = k == 0 ? b : q.x;
+        q.y = k == 1 ? b : q.y;
+        q.z = k == 2 ? b : q.z;
+        q.w = b;
+        if (k == 3 && count < cap) row[count >> 2] = q;
+        ++count;
+    }
+    // the last partial vector (its tail entries are stale and never read)
+    __device__ __forceinline__ void close(const GatherArgs &A, uint32_t a) {
+        if (!cap) return;
+        if ((count & 3u) && count <= cap) row[count >> 2] = q;
+        A.hcount[a] = count > cap ? kListOverflow : (uint16_t)count;
+    }
+};
+
+__device__ __forceinline__ void close_hits_empty(const GatherArgs &A, uint32_t a) {
+    if (A.hcap) A.hcount[a] = 0;
+}
+
+__device__ __forceinline__ bool have_hits(const GatherArgs &A, uint32_t a) {
+    return A.hcap != 0 && A.hcount[a] != kListOverflow;
+}
+
+template <class F>
+__device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const float4 *__restrict__ ps, F &&f) {
+    const uint32_t c = A.hcount[a];
+    const uint4 *row = reinterpret_cast<const uint4 *>(A.hlist + (size_t)a * A.hcap);
+    uint32_t j = 0;
+    for (; j + 4 <= c; j += 4) {
+        const uint4 b = __ldg(row + (j >> 2));
+        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
+        f(b.x, p0);
+        f(b.y, p1);
+        f(b.z, p2);
+        f(b.w, p3);
+    }
+    if (j < c) {
+        const uint4 b = __ldg(row + (j >> 2));
+        const uint32_t rest = c - j;
+        const float4 p0 = __ldg(&ps[b.x]);
+        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
+        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
+        f(b.x, p0);
+        if (rest > 1) f(b.y, p1);
+        if (rest > 2) f(b.z, p2);
+    }
+}
+
 template <int PROFILE, int MODE>
 __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
                                                 float *__restrict__ lambda, float *__restrict__ density) {
@@ -261,6 +328,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
         lambda[a] = 0.f;
         density[a] = 0.f;
         if (MODE == kBuild && A.cap) A.ncount[a] = 0;
+        close_hits_empty(A, a);
         return;
     }
     const Phys &ph = A.ph;
@@ -269,6 +337,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     const float4 pa = ps[a];
     const bool list = use_list<MODE>(A, S, a, key);
     uint32_t built = 0;
+    HitWriter hits(A, a);
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
     for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
@@ -283,6 +352,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 const float t = ph.hh - r * r;
                 rho = __fmaf_rn(pa.w, ph.poly6f * (t * t * t), rho);
                 if (r >= kKernelEpsilon) {
+                    hits.add(b);
                     const float hr = ph.h - r;
                     const float sc = ph.spikyf * ((hr * hr) / r);
                     gx = __fmaf_rn(dx * sc, ph.inv_rho0, gx);
@@ -296,6 +366,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 rho = __fmaf_rn(pb.w, t * t * t, rho);
                 const float r = sqrtf(r2);
                 if (r >= kKernelEpsilon) {
+                    hits.add(b);
                     const float hr = ph.h - r;
                     const float sc = pb.w * ((hr * hr) / r);
                     gx = __fmaf_rn(sc, dx, gx);
@@ -307,6 +378,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
         }
     });
     if (MODE == kBuild && A.cap) A.ncount[a] = built > A.cap ? kListOverflow : (uint16_t)built;
+    hits.close(A, a);
     float dens, lam;
     if (PROFILE == kRef) {
         dens = rho;
@@ -409,10 +481,9 @@ __global__ void __launch_bounds__(256)
     const Phys &ph = A.ph;
     const uint32_t key = A.keys[a];
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
-    const bool list = use_list<MODE>(A, S, a, key);
     const float la = lambda[a];
     float px = 0.f, py = 0.f, pz = 0.f;
-    for_candidates(A, S, a, key, list, ps_in, [&](uint32_t b, const float4 &pb) {
+    auto body = [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
@@ -445,7 +516,12 @@ __global__ void __launch_bounds__(256)
                 }
             }
         }
-    });
+    };
+    if (have_hits(A, a)) {
+        for_hits(A, a, ps_in, body);
+    } else {
+        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), ps_in, body);
+    }
     float world[3];
     if (PROFILE == kRef) {
         world[0] = (pa.x + px) * S.scale;
@@ -516,6 +592,7 @@ __global__ void __launch_bounds__(256)
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         omega[a] = make_float4(0.f, 0.f, 0.f, 0.f);
         vx[a] = va4;
+        close_hits_empty(A, a);
         return;
     }
     const Phys &ph = A.ph;
@@ -525,6 +602,7 @@ __global__ void __launch_bounds__(256)
     const bool list = use_list<kCheck>(A, S, a, key);
     const float va[3] = {va4.x, va4.y, va4.z};
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
+    HitWriter hits(A, a);
     for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
         if (__ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
@@ -539,6 +617,7 @@ __global__ void __launch_bounds__(256)
         xs[2] = __fmaf_rn(mw, vab[2], xs[2]);
         const float r = sqrtf(r2);
         if (r >= kKernelEpsilon) {
+            hits.add(b);
             const float hr = ph.h - r;
             const float sc = pb.w * ((hr * hr) / r);
             float cr[3];
@@ -548,6 +627,7 @@ __global__ void __launch_bounds__(256)
             o[2] = __fmaf_rn(sc, cr[2], o[2]);
         }
     });
+    hits.close(A, a);
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ws = ph.poly6f * ph.inv_rho0;
     const float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;
@@ -568,10 +648,10 @@ __global__ void __launch_bounds__(256)
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     const float4 oa = omega[a];
-    const bool list = use_list<kStored>(A, S, a, key);
     float e[3] = {0.f, 0.f, 0.f};
-    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
-        if (__ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+    // fluid_known: b came from the hit list, which holds fluid particles only
+    auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
+        if (!fluid_known && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
@@ -582,7 +662,13 @@ __global__ void __launch_bounds__(256)
         e[0] = __fmaf_rn(sc, d[0], e[0]);
         e[1] = __fmaf_rn(sc, d[1], e[1]);
         e[2] = __fmaf_rn(sc, d[2], e[2]);
-    });
+    };
+    if (have_hits(A, a)) {
+        for_hits(A, a, ps, [&](uint32_t b, const float4 &pb) { body(b, pb, true); });
+    } else {
+        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), ps,
+                       [&](uint32_t b, const float4 &pb) { body(b, pb, false); });
+    }
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ex = e[0] * gs, ey = e[1] * gs, ez = e[2] * gs;
     const float el = sqrtf(ex * ex + ey * ey + ez * ez);
@@ -671,6 +757,9 @@ GatherArgs gather_args(const StepView &s) {
     A.disp = s.disp;
     A.cellmax = s.cellmax;
     A.valid = s.valid;
+    A.hlist = s.hlist;
+    A.hcount = s.hcount;
+    A.hcap = s.hlist ? s.hcap : 0;
     return A;
 }
 

@@ -231,6 +231,9 @@ struct fgb_batch {
     Dev<float> disp;
     Dev<uint32_t> cellmax;
     Dev<uint8_t> valid;
+    Dev<uint32_t> hlist;
+    Dev<uint16_t> hcount;
+    uint32_t hit_cap = 64;
     uint32_t list_cap = 96;
     float skin_frac = 0.2f;
     Dev<float> lambda, density;
@@ -315,6 +318,9 @@ struct fgb_batch {
         s.disp = disp.p;
         s.cellmax = cellmax.p;
         s.valid = valid.p;
+        s.hlist = hlist.p;
+        s.hcount = hcount.p;
+        s.hcap = hlist.p ? hit_cap : 0;
         return s;
     }
 
@@ -640,6 +646,13 @@ static int batch_init(fgb_batch *b) {
         FGB_CUDA(b->valid.alloc(n), "batch alloc");
         FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
     }
+    if (const char *e = getenv("FGB_HIT_CAP")) b->hit_cap = (uint32_t)atoi(e);
+    if (b->hit_cap > 4096) b->hit_cap = 4096;
+    b->hit_cap = (b->hit_cap + 3u) & ~3u;  // rows move as 16-byte vectors
+    if (b->hit_cap) {
+        FGB_CUDA(b->hlist.alloc(n * b->hit_cap), "batch alloc hit lists");
+        FGB_CUDA(b->hcount.alloc(n), "batch alloc");
+    }
     FGB_CUDA(b->lambda.alloc(n), "batch alloc");
     FGB_CUDA(b->density.alloc(n), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
@@ -756,12 +769,14 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
 
 // Device bytes a batch allocates for one scene (admission control of the serving
 // loop): per-particle arrays, the scene's cell table, and the surface buffers when a
-// mesh is wanted (triangles estimated at one per 20 cubes).
-static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64_t n, bool mesh, uint32_t cap) {
+// mesh is wanted (triangles estimated at one per 20 cubes).  list_words: Verlet-list
+// plus hit-list entries per particle.
+static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64_t n, bool mesh,
+                                uint32_t list_words) {
     SceneDev S{};
     scene_geometry(p, c, S);
     const uint64_t table = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
-    uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * cap + 2 + 4 + 1;
+    uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * list_words + 2 + 2 + 4 + 1;
     if (p.profile != FGB_PROFILE_REF) per_particle += 32;
     uint64_t bytes = per_particle * n + 12 * table;
     if (mesh && S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1) {
@@ -1162,9 +1177,10 @@ int fgb_batch_copy_scene(fgb_batch *dst, uint32_t dst_scene, fgb_batch *src, uin
 
 int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, int want_mesh, uint64_t *bytes) {
     if (!s || !cfg || !bytes) return fail(FGB_ERR_INVALID, "footprint: bad argument");
-    uint32_t cap = 96;
+    uint32_t cap = 96, hits = 64;
     if (const char *e = getenv("FGB_LIST_CAP")) cap = (uint32_t)atoi(e);
-    *bytes = scene_footprint(s->params, *cfg, n, want_mesh != 0, cap);
+    if (const char *e = getenv("FGB_HIT_CAP")) hits = (uint32_t)atoi(e);
+    *bytes = scene_footprint(s->params, *cfg, n, want_mesh != 0, cap + hits);
     return FGB_OK;
 }
 
