@@ -55,8 +55,9 @@ struct StepView {
     float4 *omega, *vx;
     uint32_t *err;
     int block;             // threads per CTA of the gather kernels
-    // per-step neighbour lists (Verlet lists with a skin), slot-major: list[j * n + a]
-    uint32_t *nlist;       // cap * n candidate indices, in 27-cell walk order
+    // per-step neighbour lists (Verlet lists with a skin), particle-major rows of cap
+    // entries (cap a multiple of 4): list[a * cap + j]
+    uint32_t *nlist;       // n * cap candidate indices, in 27-cell walk order
     uint16_t *ncount;      // entries per particle (kListOverflow: walk the cells)
     uint32_t cap;          // list capacity per particle (0: lists disabled)
     float list_r2;         // (h + skin)^2: candidates kept at build time
@@ -67,8 +68,8 @@ struct StepView {
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
     // per-pass hit lists: the candidates of one pass that lie within h (and not on top
     // of the particle), in walk order; written by a lambda / vorticity pass, read by the
-    // delta / vorticity-apply pass over the same positions.  Slot-major like nlist.
-    uint32_t *hlist;       // hcap * n
+    // delta / vorticity-apply pass over the same positions.  Rows like nlist.
+    uint32_t *hlist;       // n * hcap
     uint16_t *hcount;      // entries per particle (kListOverflow: use nlist / the cells)
     uint32_t hcap;
 };
@@ -81,6 +82,9 @@ void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
                   cudaStream_t st);
+// ref-profile colour diffusion of the sorted colours (col1, in place); agg and count
+// are n-entry scratch arrays
+void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st);
 // `between` runs after the first of the two kernels (stage timing hook)
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
                            const std::function<void()> &between = nullptr);

@@ -5,6 +5,7 @@
 //   radix sort       (sort.cu)                              (oclsph.hpp:733-743)
 //   k_reorder_cells  gather the state into sorted SoA float4 and write each cell's
 //                    {start, end} by adjacent difference    (oclsph.hpp:746-767, 822-853)
+//   ref only:        k_cell_colours, k_diffuse              (oclsph_kernel.h:281-303)
 //   iterations x {k_lambda, k_delta}                        (oclsph_kernel.h:305-384)
 //   k_delta(last)    also finalises x / v                   (oclsph_kernel.h:404-416)
 //   baseline only:   k_vorticity_xsph, k_vorticity_apply    (PBF paper eq. 15-17)
@@ -211,28 +212,39 @@ __device__ __forceinline__ void visit_range(uint32_t lo, uint32_t hi, const floa
     for (; b < hi; ++b) f(b, __ldg(&ps[b]));
 }
 
+// Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
+// a multiple of 4) as f(b, p_b); indices arrive four at a time as one 16-byte load,
+// and the four positions are loaded before any arithmetic.
+template <class F>
+__device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
+                                        const float4 *__restrict__ ps, F &f) {
+    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
+    uint32_t j = 0;
+    for (; j + 4 <= c; j += 4) {
+        const uint4 b = __ldg(row + (j >> 2));
+        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
+        f(b.x, p0);
+        f(b.y, p1);
+        f(b.z, p2);
+        f(b.w, p3);
+    }
+    if (j < c) {
+        const uint4 b = __ldg(row + (j >> 2));
+        const uint32_t rest = c - j;
+        const float4 p0 = __ldg(&ps[b.x]);
+        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
+        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
+        f(b.x, p0);
+        if (rest > 1) f(b.y, p1);
+        if (rest > 2) f(b.z, p2);
+    }
+}
+
 template <class F>
 __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
                                                bool list, const float4 *__restrict__ ps, F &&f) {
     if (list) {
-        const uint32_t c = A.ncount[a];
-        const uint32_t *L = A.nlist + a;
-        const size_t n = A.n;
-        uint32_t j = 0;
-        for (; j + kPrefetch <= c; j += kPrefetch) {
-            uint32_t b[kPrefetch];
-            float4 p[kPrefetch];
-#pragma unroll
-            for (int k = 0; k < kPrefetch; ++k) b[k] = __ldg(L + (size_t)(j + k) * n);
-#pragma unroll
-            for (int k = 0; k < kPrefetch; ++k) p[k] = __ldg(&ps[b[k]]);
-#pragma unroll
-            for (int k = 0; k < kPrefetch; ++k) f(b[k], p[k]);
-        }
-        for (; j < c; ++j) {
-            const uint32_t b = __ldg(L + (size_t)j * n);
-            f(b, __ldg(&ps[b]));
-        }
+        for_row(A.nlist, A.cap, a, A.ncount[a], ps, f);
     } else {
         const uint32_t m = morton_of(key, A.mbits);
         const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
@@ -261,14 +273,13 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 // list, and the second iterates it: about 35 entries instead of the ~60 of the Verlet
 // list or the ~216 of the cell walk, with no lanes idling on the range test.  The
 // second pass still applies its own range tests to each hit, so its sums are
-// bit-identical to a walk.  Rows are particle-major (hcap entries, hcap a multiple of
-// 4) and move as 16-byte vectors: four hits per store and per load.
-struct HitWriter {
+// bit-identical to a walk.  Rows are particle-major like the Verlet lists.
+struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
     uint4 q;
-    __device__ __forceinline__ HitWriter(const GatherArgs &A, uint32_t a)
-        : row(reinterpret_cast<uint4 *>(A.hlist + (size_t)a * A.hcap)), cap(A.hcap) {}
+    __device__ __forceinline__ RowWriter(uint32_t *base, uint32_t cap_, uint32_t a)
+        : row(reinterpret_cast<uint4 *>(base + (size_t)a * cap_)), cap(cap_) {}
     __device__ __forceinline__ void add(uint32_t b) {
         const uint32_t k = count & 3u;
         q.x = k == 0 ? b : q.x;
@@ -278,11 +289,18 @@ struct HitWriter {
         if (k == 3 && count < cap) row[count >> 2] = q;
         ++count;
     }
-    // the last partial vector (its tail entries are stale and never read)
-    __device__ __forceinline__ void close(const GatherArgs &A, uint32_t a) {
-        if (!cap) return;
+    // store the last partial vector (its tail entries are stale and never read);
+    // returns the row's count, kListOverflow when it did not fit
+    __device__ __forceinline__ uint16_t close() {
         if ((count & 3u) && count <= cap) row[count >> 2] = q;
-        A.hcount[a] = count > cap ? kListOverflow : (uint16_t)count;
+        return count > cap ? kListOverflow : (uint16_t)count;
+    }
+};
+
+struct HitWriter : RowWriter {
+    __device__ __forceinline__ HitWriter(const GatherArgs &A, uint32_t a) : RowWriter(A.hlist, A.hcap, a) {}
+    __device__ __forceinline__ void close(const GatherArgs &A, uint32_t a) {
+        if (cap) A.hcount[a] = RowWriter::close();
     }
 };
 
@@ -296,27 +314,7 @@ __device__ __forceinline__ bool have_hits(const GatherArgs &A, uint32_t a) {
 
 template <class F>
 __device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const float4 *__restrict__ ps, F &&f) {
-    const uint32_t c = A.hcount[a];
-    const uint4 *row = reinterpret_cast<const uint4 *>(A.hlist + (size_t)a * A.hcap);
-    uint32_t j = 0;
-    for (; j + 4 <= c; j += 4) {
-        const uint4 b = __ldg(row + (j >> 2));
-        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
-        f(b.x, p0);
-        f(b.y, p1);
-        f(b.z, p2);
-        f(b.w, p3);
-    }
-    if (j < c) {
-        const uint4 b = __ldg(row + (j >> 2));
-        const uint32_t rest = c - j;
-        const float4 p0 = __ldg(&ps[b.x]);
-        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
-        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
-        f(b.x, p0);
-        if (rest > 1) f(b.y, p1);
-        if (rest > 2) f(b.z, p2);
-    }
+    for_row(A.hlist, A.hcap, a, A.hcount[a], ps, f);
 }
 
 template <int PROFILE, int MODE>
@@ -336,15 +334,14 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     const bool list = use_list<MODE>(A, S, a, key);
-    uint32_t built = 0;
+    RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
     HitWriter hits(A, a);
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
     for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (MODE == kBuild && A.cap && r2 <= A.list_r2) {
-            if (built < A.cap) A.nlist[(size_t)built * A.n + a] = b;
-            ++built;
+            built.add(b);
         }
         if (PROFILE == kRef) {
             const float r = sqrtf(r2);
@@ -377,7 +374,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             }
         }
     });
-    if (MODE == kBuild && A.cap) A.ncount[a] = built > A.cap ? kListOverflow : (uint16_t)built;
+    if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
     hits.close(A, a);
     float dens, lam;
     if (PROFILE == kRef) {
@@ -689,6 +686,85 @@ __global__ void __launch_bounds__(256)
     x[a] = make_float4(pa.x * S.scale, pa.y * S.scale, pa.z * S.scale, xa.w);
 }
 
+// Colour diffusion of the ref profile (oclsph_kernel.h:281-303): each fluid particle
+// averages the colours of every fluid candidate in its 27 cells (no distance test,
+// itself included) and moves toward 1.33x that mean by dt/750, per 8-bit channel,
+// clamped to [8, 255] and truncated.  The channel sums are integers below 2^24, exact
+// in float in any order, so each cell's sums are formed once (k_cell_colours, at the
+// cell's first sorted index) and a particle adds up 27 of them.
+__global__ void k_cell_colours(uint32_t n, const uint32_t *__restrict__ keys, const int32_t *__restrict__ type,
+                               const uint32_t *__restrict__ col, uint4 *__restrict__ agg,
+                               uint32_t *__restrict__ count) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t key = keys[i];
+        if (i > 0 && keys[i - 1] == key) continue;
+        uint4 s = make_uint4(0, 0, 0, 0);
+        uint32_t c = 0;
+        for (uint32_t j = i; j < n && keys[j] == key; ++j) {
+            if (type[j] == FGB_TYPE_OBSTACLE) continue;
+            const uint32_t v = col[j];
+            s.x += v & 0xffu;
+            s.y += (v >> 8) & 0xffu;
+            s.z += (v >> 16) & 0xffu;
+            s.w += v >> 24;
+            ++c;
+        }
+        agg[i] = s;
+        count[i] = c;
+    }
+}
+
+// OpenCL mix(x, y, t) = x + (y - x) t, then clamp and convert_uchar (round to zero)
+__device__ __forceinline__ uint32_t diffuse_channel(uint32_t own, uint32_t sum, float count, float t) {
+    const float x = (float)own;
+    const float y = ((float)sum / count) * 1.33f;
+    float o = x + (y - x) * t;
+    o = fminf(fmaxf(o, 8.f), 255.f);
+    return (uint32_t)o;
+}
+
+__global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint32_t mbits,
+                          const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
+                          const int32_t *__restrict__ type, const uint4 *__restrict__ agg,
+                          const uint32_t *__restrict__ count, uint32_t *__restrict__ col) {
+    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+        if (type[a] == FGB_TYPE_OBSTACLE) continue;
+        const uint32_t key = keys[a];
+        const SceneDev &S = scenes[scene_of(key, mbits)];
+        const uint32_t m = morton_of(key, mbits);
+        const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
+        const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+        const uint2 *tbl = cells + S.table_base;
+        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+        uint4 s = make_uint4(0, 0, 0, 0);
+        uint32_t c = 0;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int z = cz + dz;
+            if (z < 0 || z > ez) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy + dy;
+                if (y < 0 || y > ey) continue;
+                const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
+                for (int x = x0; x <= x1; ++x) {
+                    const uint2 r = __ldg(&tbl[spread10((uint32_t)x) | yz]);
+                    if (r.x >= r.y) continue;
+                    const uint4 g = __ldg(&agg[r.x]);
+                    s.x += g.x;
+                    s.y += g.y;
+                    s.z += g.z;
+                    s.w += g.w;
+                    c += __ldg(&count[r.x]);
+                }
+            }
+        }
+        const float t = S.dt / 750.f;
+        const float fc = (float)c;
+        const uint32_t v = col[a];
+        col[a] = diffuse_channel(v & 0xffu, s.x, fc, t) | (diffuse_channel((v >> 8) & 0xffu, s.y, fc, t) << 8) |
+                 (diffuse_channel((v >> 16) & 0xffu, s.z, fc, t) << 16) | (diffuse_channel(v >> 24, s.w, fc, t) << 24);
+    }
+}
+
 // Keys of the current positions (marching-cubes grid).
 __global__ void k_position_keys(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
                                 const uint32_t *__restrict__ keys_prev, const float4 *__restrict__ x,
@@ -824,6 +900,12 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
     k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
     if (between) between();
     k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1);
+}
+
+void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {
+    k_cell_colours<<<stream_grid(s.n), 256, 0, st>>>(s.n, s.keys_sorted, s.type1, s.col1, agg, count);
+    k_diffuse<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.n, s.mbits, s.keys_sorted, s.cells, s.type1, agg, count,
+                                                s.col1);
 }
 
 void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st) {

@@ -238,6 +238,8 @@ struct fgb_batch {
     float skin_frac = 0.2f;
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
+    Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
+    Dev<uint32_t> colour_count;
     Dev<uint32_t> err;
     // surface
     bool surf_ready = false;
@@ -355,6 +357,10 @@ struct fgb_batch {
         if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
+        if (ph.profile == FGB_PROFILE_REF) {
+            launch_diffuse(s, colour_sums.p, colour_count.p, st);
+            l += 2;
+        }
         mark(k, st);
         // p* of the grid stays in ps_grid; the iterations ping-pong between ps[0] and ps[1]
         const float4 *pin = ps_grid.p;
@@ -639,6 +645,7 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_LIST_CAP")) b->list_cap = (uint32_t)atoi(e);
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
     if (b->list_cap > 4096) b->list_cap = 4096;
+    b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
     if (b->list_cap) {
         FGB_CUDA(b->nlist.alloc(n * b->list_cap), "batch alloc neighbour lists");
         FGB_CUDA(b->ncount.alloc(n), "batch alloc");
@@ -658,6 +665,9 @@ static int batch_init(fgb_batch *b) {
     if (p.profile != FGB_PROFILE_REF) {
         FGB_CUDA(b->omega.alloc(n), "batch alloc");
         FGB_CUDA(b->vx.alloc(n), "batch alloc");
+    } else {
+        FGB_CUDA(b->colour_sums.alloc(n), "batch alloc");
+        FGB_CUDA(b->colour_count.alloc(n), "batch alloc");
     }
     FGB_CUDA(b->err.alloc(1), "batch alloc");
     FGB_CUDA(b->d_scenes.alloc(b->n_scenes), "batch alloc");
@@ -777,7 +787,7 @@ static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64
     scene_geometry(p, c, S);
     const uint64_t table = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
     uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * list_words + 2 + 2 + 4 + 1;
-    if (p.profile != FGB_PROFILE_REF) per_particle += 32;
+    per_particle += p.profile != FGB_PROFILE_REF ? 32 : 20;
     uint64_t bytes = per_particle * n + 12 * table;
     if (mesh && S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1) {
         const uint64_t samples = (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];

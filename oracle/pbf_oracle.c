@@ -356,6 +356,43 @@ typedef struct state {
     const float *mass;
 } state;
 
+/* oclsph_kernel.h:281-303 (ref profile only): every fluid particle averages the
+ * colours of all fluid candidates of its 27 cells (no distance test, itself
+ * included) and moves toward 1.33x the mean by dt/750 per 8-bit channel:
+ * OpenCL mix(x, y, t) = x + (y - x) t, clamp to [8, 255], convert_uchar rounds to
+ * zero.  Channel sums are integers below 2^24, exact in float, so summing them as
+ * integers gives the reference's float4 accumulation in any order. */
+static void diffuse_colours(const state *s, uint32_t *colour) {
+    const size_t n = s->n;
+    uint32_t *out = (uint32_t *)malloc(n * sizeof(uint32_t));
+    const float t = s->c->dt / 750.f;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < (long)n; ++i) {
+        out[i] = colour[i];
+        if (s->type[i] == FGB_TYPE_OBSTACLE) continue;
+        ranges rg;
+        neighbour_ranges(&s->g, s->cells, s->cxyz[3 * i], s->cxyz[3 * i + 1], s->cxyz[3 * i + 2], &rg);
+        uint32_t sum[4] = {0, 0, 0, 0}, cnt = 0;
+        for (int r = 0; r < rg.n; ++r)
+            for (uint32_t b = rg.r[r][0]; b < rg.r[r][1]; ++b) {
+                if (s->type[b] == FGB_TYPE_OBSTACLE) continue;
+                for (int ch = 0; ch < 4; ++ch) sum[ch] += (colour[b] >> (8 * ch)) & 0xffu;
+                ++cnt;
+            }
+        uint32_t v = 0;
+        for (int ch = 0; ch < 4; ++ch) {
+            const float x = (float)((colour[i] >> (8 * ch)) & 0xffu);
+            const float y = ((float)sum[ch] / (float)cnt) * 1.33f;
+            float o = x + (y - x) * t;
+            o = fminf(fmaxf(o, 8.f), 255.f);
+            v |= (uint32_t)o << (8 * ch);
+        }
+        out[i] = v;
+    }
+    memcpy(colour, out, n * sizeof(uint32_t));
+    free(out);
+}
+
 /* oclsph_kernel.h:305-332 (ref) / PBF paper eq. 8-11 (baseline). */
 static void lambda_pass(const state *s, const float *ps, float *lam, float *rho_out) {
     const kc *k = &s->k;
@@ -662,6 +699,8 @@ int orc_step(const fgb_params *p, const fgb_config *c, size_t n, uint64_t *id, i
     s.cxyz = cxyz;
     s.type = type;
     s.mass = mass;
+
+    if (p->profile == FGB_PROFILE_REF) diffuse_colours(&s, colour);
 
     float *lam = (float *)calloc(n, sizeof(float));
     float *rho = (float *)calloc(n, sizeof(float));
