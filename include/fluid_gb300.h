@@ -217,19 +217,22 @@ int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, 
 /* ---- serving: a resident request loop with continuous batching ---------- */
 /* A worker thread admits requests in arrival order while the sum of their device
  * footprints (fgb_scene_footprint) stays within half the budget (a membership
- * change briefly holds two batches), keeps admitted scenes resident, and advances
- * all of them together, one batched step per tick.  Finished scenes optionally
- * get a surface; their final state waits on the host for fgb_serve_fetch.  Every
- * request of one server must use the same iteration count.  While a server runs,
- * its solver must not be used for other calls. */
+ * change briefly holds two batches) and keeps admitted scenes resident.  Resident
+ * scenes are packed into groups of at most tick_particles particles; a tick
+ * advances one group by one batched step, the groups taken round robin.  Finished
+ * scenes optionally get a surface; their final state waits on the host for
+ * fgb_serve_fetch.  Every request of one server must use the same iteration count.
+ * While a server runs, its solver must not be used for other calls. */
 #define FGB_SERVE_WAITING 0
 #define FGB_SERVE_ACTIVE  1
 #define FGB_SERVE_DONE    2 /* negative status: the FGB_ERR_* that failed the request */
 
 typedef struct fgb_serve_options {
     uint64_t budget_bytes;   /* HBM budget (0: 150 GiB) */
-    uint32_t max_active;     /* most scenes in one batch (0: 256) */
+    uint32_t max_active;     /* most resident scenes (0: 256) */
     uint32_t one_at_a_time;  /* 1: no batching, one scene at a time (the comparison loop) */
+    uint64_t tick_particles; /* most particles stepped in one tick (0: 2 097 152); a
+                                larger scene is stepped alone */
 } fgb_serve_options;
 
 typedef struct fgb_serve_result {

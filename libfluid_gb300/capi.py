@@ -132,6 +132,7 @@ class ServeOptions(ctypes.Structure):
         ("budget_bytes", ctypes.c_uint64),
         ("max_active", ctypes.c_uint32),
         ("one_at_a_time", ctypes.c_uint32),
+        ("tick_particles", ctypes.c_uint64),
     ]
 
 

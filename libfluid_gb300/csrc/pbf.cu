@@ -215,13 +215,16 @@ __device__ __forceinline__ void visit_range(uint32_t lo, uint32_t hi, const floa
 // Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
 // a multiple of 4) as f(b, p_b); indices arrive four at a time as one 16-byte load,
 // and the four positions are loaded before any arithmetic.
-template <class F>
+// kSameKernel: the row was written earlier in this kernel, so it is read through L2
+// (ld.global.cg) rather than the read-only path.
+template <bool kSameKernel = false, class F>
 __device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
                                         const float4 *__restrict__ ps, F &f) {
     const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
+    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
     uint32_t j = 0;
     for (; j + 4 <= c; j += 4) {
-        const uint4 b = __ldg(row + (j >> 2));
+        const uint4 b = load(j);
         const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
         f(b.x, p0);
         f(b.y, p1);
@@ -229,7 +232,7 @@ __device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint3
         f(b.w, p3);
     }
     if (j < c) {
-        const uint4 b = __ldg(row + (j >> 2));
+        const uint4 b = load(j);
         const uint32_t rest = c - j;
         const float4 p0 = __ldg(&ps[b.x]);
         const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
@@ -269,11 +272,14 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 
 // Hit lists.  A lambda pass and the delta pass after it read the same p*, so they
 // agree on which candidates lie within h; likewise the two vorticity passes.  The
-// first pass of each pair appends those candidates (in walk order) to a per-pass hit
-// list, and the second iterates it: about 35 entries instead of the ~60 of the Verlet
-// list or the ~216 of the cell walk, with no lanes idling on the range test.  The
-// second pass still applies its own range tests to each hit, so its sums are
-// bit-identical to a walk.  Rows are particle-major like the Verlet lists.
+// first pass of each pair filters its candidates (Verlet list or cell walk) by range
+// alone, appending those within h (in walk order) to a per-pass hit list, then runs
+// its kernel arithmetic over the hits; the second pass of the pair iterates the same
+// hits.  About 35 entries instead of the ~60 of the Verlet list or the ~216 of the
+// cell walk, and no lanes idle on a range test during the arithmetic.  Every pass
+// still applies its own range tests to each hit, so its sums are bit-identical to a
+// walk.  A row that overflows (count > hcap) sends its passes back to the candidates.
+// Rows are particle-major like the Verlet lists.
 struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
@@ -334,22 +340,16 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     const bool list = use_list<MODE>(A, S, a, key);
-    RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
-    HitWriter hits(A, a);
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
-    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+    auto body = [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        if (MODE == kBuild && A.cap && r2 <= A.list_r2) {
-            built.add(b);
-        }
         if (PROFILE == kRef) {
             const float r = sqrtf(r2);
             if (r <= ph.h) {
                 const float t = ph.hh - r * r;
                 rho = __fmaf_rn(pa.w, ph.poly6f * (t * t * t), rho);
                 if (r >= kKernelEpsilon) {
-                    hits.add(b);
                     const float hr = ph.h - r;
                     const float sc = ph.spikyf * ((hr * hr) / r);
                     gx = __fmaf_rn(dx * sc, ph.inv_rho0, gx);
@@ -363,7 +363,6 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 rho = __fmaf_rn(pb.w, t * t * t, rho);
                 const float r = sqrtf(r2);
                 if (r >= kKernelEpsilon) {
-                    hits.add(b);
                     const float hr = ph.h - r;
                     const float sc = pb.w * ((hr * hr) / r);
                     gx = __fmaf_rn(sc, dx, gx);
@@ -373,9 +372,26 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 }
             }
         }
-    });
-    if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
-    hits.close(A, a);
+    };
+    if (A.hcap == 0 && MODE != kBuild) {
+        for_candidates(A, S, a, key, list, ps, body);
+    } else {
+        // phase 1: range filter (and the Verlet list on the build pass)
+        RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
+        HitWriter hits(A, a);
+        for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+            const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
+            const bool in = PROFILE == kRef ? sqrtf(r2) <= ph.h : r2 <= ph.hh;
+            if (in) hits.add(b);
+        });
+        if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
+        hits.close(A, a);
+        // phase 2: the kernel arithmetic over the hits, in walk order
+        if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, ps, body);
+        else for_candidates(A, S, a, key, list, ps, body);
+    }
     float dens, lam;
     if (PROFILE == kRef) {
         dens = rho;
@@ -599,9 +615,9 @@ __global__ void __launch_bounds__(256)
     const bool list = use_list<kCheck>(A, S, a, key);
     const float va[3] = {va4.x, va4.y, va4.z};
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
-    HitWriter hits(A, a);
-    for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
-        if (__ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+    // fluid_known: b came from the hit list, which holds fluid particles only
+    auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
+        if (!fluid_known && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
@@ -614,7 +630,6 @@ __global__ void __launch_bounds__(256)
         xs[2] = __fmaf_rn(mw, vab[2], xs[2]);
         const float r = sqrtf(r2);
         if (r >= kKernelEpsilon) {
-            hits.add(b);
             const float hr = ph.h - r;
             const float sc = pb.w * ((hr * hr) / r);
             float cr[3];
@@ -623,8 +638,26 @@ __global__ void __launch_bounds__(256)
             o[1] = __fmaf_rn(sc, cr[1], o[1]);
             o[2] = __fmaf_rn(sc, cr[2], o[2]);
         }
-    });
-    hits.close(A, a);
+    };
+    auto any = [&](uint32_t b, const float4 &pb) { body(b, pb, false); };
+    if (A.hcap == 0) {
+        for_candidates(A, S, a, key, list, ps, any);
+    } else {
+        // phase 1: fluid candidates within h; phase 2: the arithmetic over them
+        HitWriter hits(A, a);
+        for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+            const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 <= ph.hh && __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE) hits.add(b);
+        });
+        hits.close(A, a);
+        if (hits.count <= A.hcap) {
+            auto fluid = [&](uint32_t b, const float4 &pb) { body(b, pb, true); };
+            for_row<true>(A.hlist, A.hcap, a, hits.count, ps, fluid);
+        } else {
+            for_candidates(A, S, a, key, list, ps, any);
+        }
+    }
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ws = ph.poly6f * ph.inv_rho0;
     const float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;

@@ -882,7 +882,8 @@ const char *fgb_last_error(void) { return g_last_error.c_str(); }
 int fgb_struct_sizes(uint64_t *out, int n) {
     const uint64_t sizes[] = {sizeof(fgb_params), sizeof(fgb_config),        sizeof(fgb_particles),
                               sizeof(fgb_triangle), sizeof(fgb_mesh_triangle), sizeof(fgb_mesh),
-                              sizeof(fgb_grid_info), sizeof(fgb_well)};
+                              sizeof(fgb_grid_info), sizeof(fgb_well),          sizeof(fgb_serve_options),
+                              sizeof(fgb_serve_result), sizeof(fgb_serve_stats)};
     const int m = (int)(sizeof(sizes) / sizeof(sizes[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = sizes[i];
     return m;

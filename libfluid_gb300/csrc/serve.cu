@@ -2,16 +2,18 @@
 //
 // Requests (a scene, a step count, optionally a final surface) arrive at any time.
 // A worker thread admits waiting requests in arrival order while their device
-// footprint fits the HBM budget, keeps every admitted scene resident on the device,
-// and advances all active scenes together: one tick = one step of one batch, i.e.
-// one launch per stage for every scene (fgb_batch_step).  When scenes finish or are
-// admitted, the survivors are copied device-to-device into a new batch with the new
-// membership (fgb_batch_copy_scene keeps their particle order, so a scene's result
-// is bit-identical alone and in any mix).  Finished scenes optionally run marching
-// cubes, their final state is copied to the host, and their memory is released.
+// footprint fits the HBM budget and keeps every admitted scene resident on the
+// device.  Admitted scenes are packed first-fit into groups of at most
+// tick_particles particles; one tick advances one group by one step (one launch per
+// stage for all its scenes, fgb_batch_step), taking the groups round robin, so a
+// tick costs about the same whatever the mix.  When a group's membership changes,
+// its survivors are copied device-to-device into a new batch (fgb_batch_copy_scene
+// keeps their particle order, so a scene's result is bit-identical alone and in any
+// mix).  Finished scenes optionally run marching cubes, their final state is copied
+// to the host, and their memory is released.
 //
-// Budget accounting: a membership change holds the old and the new batch at once,
-// so admission keeps the sum of active footprints within half the budget.
+// Budget accounting: rebuilding a group holds its old and new batch at once, so
+// admission keeps the sum of active footprints within half the budget.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -65,6 +67,18 @@ struct Request {
 
 }  // namespace
 
+// Scenes that are stepped together: one batch (one launch per stage for all of
+// them).  A group holds at most tick_particles particles (a larger scene is a group
+// on its own), so every tick does about the same amount of work whatever the mix of
+// active requests -- the step latency stays flat while requests come and go.
+struct ServeGroup {
+    fgb_batch *batch = nullptr;
+    std::vector<Request *> scenes;  // scene k of `batch` is scenes[k]
+    std::vector<Request *> want;    // membership for the next tick
+    uint64_t particles = 0;         // of `want`
+    uint32_t mbits = 0;             // largest Morton key width in `want`
+};
+
 struct fgb_server {
     fgb_solver *solver = nullptr;
     fgb_serve_options opt{};
@@ -78,8 +92,8 @@ struct fgb_server {
     bool stop = false;
     double t0 = 0;
     // worker-only state
-    fgb_batch *batch = nullptr;
-    std::vector<Request *> batch_scenes;  // scene k of `batch` is batch_scenes[k]
+    std::vector<std::unique_ptr<ServeGroup>> groups;
+    size_t next_group = 0;  // round-robin position
     std::thread worker;
     // statistics (under mu)
     uint64_t ticks = 0, particle_steps = 0, completed = 0, rejected = 0, failed = 0, rebuilds = 0;
@@ -89,11 +103,10 @@ struct fgb_server {
 
     double t() const { return now_s() - t0; }
 
-    // Admit waiting requests (mu held); returns the scenes of the next tick.
+    // Admit waiting requests (mu held); returns the newly admitted ones.
     std::vector<Request *> admit() {
         const uint64_t cap_bytes = opt.budget_bytes / 2;
-        uint32_t mbits = 0;
-        for (Request *r : live) mbits = std::max(mbits, r->mbits);
+        std::vector<Request *> fresh;
         while (!waiting.empty()) {
             Request *r = waiting.front();
             if (r->footprint > cap_bytes) {  // could never fit
@@ -105,37 +118,55 @@ struct fgb_server {
             }
             if (opt.one_at_a_time && !live.empty()) break;
             if (live.size() >= opt.max_active) break;
-            const uint32_t mb = std::max(mbits, r->mbits);
-            if (mb + bits_of((uint32_t)live.size()) > 32) break;  // scene id above the Morton key
             if (used + r->footprint > cap_bytes) break;
             waiting.pop_front();
             used += r->footprint;
-            mbits = mb;
             r->status = FGB_SERVE_ACTIVE;
             r->t_admit = t();
             live.push_back(r);
+            fresh.push_back(r);
         }
-        return live;
+        return fresh;
     }
 
-    // Make `batch` hold exactly `next`; survivors move on the device.
-    int rebuild(const std::vector<Request *> &next) {
+    // First group with room for r (particles, and scene-id bits above the Morton
+    // key), else a new group.
+    void place(Request *r) {
+        for (auto &g : groups) {
+            if (opt.one_at_a_time && !g->want.empty()) continue;
+            if (!g->want.empty() && g->particles + r->n > opt.tick_particles) continue;
+            const uint32_t mb = std::max(g->mbits, r->mbits);
+            if (mb + bits_of((uint32_t)g->want.size()) > 32) continue;
+            g->want.push_back(r);
+            g->particles += r->n;
+            g->mbits = mb;
+            return;
+        }
+        auto g = std::make_unique<ServeGroup>();
+        g->want.push_back(r);
+        g->particles = r->n;
+        g->mbits = r->mbits;
+        groups.push_back(std::move(g));
+    }
+
+    // Make g.batch hold exactly g.want; survivors move on the device.
+    int rebuild(ServeGroup &g) {
         const double r0 = now_s();
         fgb_batch *nb = nullptr;
-        if (!next.empty()) {
+        if (!g.want.empty()) {
             std::vector<uint64_t> counts;
             std::vector<fgb_config> cfgs;
-            for (Request *r : next) {
+            for (Request *r : g.want) {
                 counts.push_back(r->n);
                 cfgs.push_back(r->cfg);
             }
-            int rc = fgb_batch_create(solver, (uint32_t)next.size(), counts.data(), cfgs.data(), &nb);
+            int rc = fgb_batch_create(solver, (uint32_t)g.want.size(), counts.data(), cfgs.data(), &nb);
             if (rc) return rc;
-            for (size_t k = 0; k < next.size(); ++k) {
-                Request *r = next[k];
-                auto it = std::find(batch_scenes.begin(), batch_scenes.end(), r);
-                if (it != batch_scenes.end()) {
-                    rc = fgb_batch_copy_scene(nb, (uint32_t)k, batch, (uint32_t)(it - batch_scenes.begin()));
+            for (size_t k = 0; k < g.want.size(); ++k) {
+                Request *r = g.want[k];
+                auto it = std::find(g.scenes.begin(), g.scenes.end(), r);
+                if (it != g.scenes.end()) {
+                    rc = fgb_batch_copy_scene(nb, (uint32_t)k, g.batch, (uint32_t)(it - g.scenes.begin()));
                 } else {
                     fgb_particles v = r->view();
                     rc = fgb_batch_upload(nb, (uint32_t)k, &v);
@@ -146,108 +177,133 @@ struct fgb_server {
                 }
             }
         }
-        if (batch) fgb_batch_destroy(batch);
-        batch = nb;
-        batch_scenes = next;
+        if (g.batch) fgb_batch_destroy(g.batch);
+        g.batch = nb;
+        g.scenes = g.want;
         std::lock_guard<std::mutex> lk(mu);
         rebuilds++;
         rebuild_time += now_s() - r0;
         return FGB_OK;
     }
 
-    void fail_scenes(const std::vector<Request *> &scenes, int rc) {
+    // Fail every active scene of g and empty it.
+    void fail_group(ServeGroup &g, int rc) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            last_error = fgb_last_error();
+            for (Request *r : g.want) {
+                if (r->status != FGB_SERVE_ACTIVE) continue;
+                r->status = -rc;
+                r->t_done = t();
+                used -= r->footprint;
+                failed++;
+            }
+            std::vector<Request *> keep;
+            for (Request *r : live)
+                if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
+            live.swap(keep);
+            cv.notify_all();
+        }
+        if (g.batch) fgb_batch_destroy(g.batch);
+        g.batch = nullptr;
+        g.scenes.clear();
+        g.want.clear();
+        g.particles = 0;
+    }
+
+    // One tick: step group g once; finished scenes run their surface and go home.
+    void tick(ServeGroup &g) {
+        const double s0 = now_s();
+        int rc = fgb_batch_step(g.batch, 1);
+        if (!rc) rc = fgb_batch_sync(g.batch);
+        const double s1 = now_s();
+        if (rc) return fail_group(g, rc);
+        std::vector<Request *> done;
+        for (size_t k = 0; k < g.scenes.size(); ++k) {
+            Request *r = g.scenes[k];
+            if (--r->remaining) continue;
+            if (r->want_mesh) {
+                rc = fgb_batch_surface(g.batch, (uint32_t)k, &r->mesh);
+                if (rc) return fail_group(g, rc);
+                r->triangles = r->mesh.n;
+            }
+            fgb_particles v = r->view();
+            rc = fgb_batch_download(g.batch, (uint32_t)k, &v);
+            if (rc) return fail_group(g, rc);
+            done.push_back(r);
+        }
+        if (!done.empty()) {
+            std::vector<Request *> keep;
+            g.particles = 0;
+            g.mbits = 0;
+            for (Request *r : g.want)
+                if (std::find(done.begin(), done.end(), r) == done.end()) {
+                    keep.push_back(r);
+                    g.particles += r->n;
+                    g.mbits = std::max(g.mbits, r->mbits);
+                }
+            g.want.swap(keep);
+        }
         std::lock_guard<std::mutex> lk(mu);
-        last_error = fgb_last_error();
-        for (Request *r : scenes) {
-            if (r->status != FGB_SERVE_ACTIVE) continue;
-            r->status = -rc;
+        step_latency.push_back(s1 - s0);
+        busy += s1 - s0;
+        ticks++;
+        for (Request *r : g.scenes) particle_steps += r->n;
+        for (Request *r : done) {
+            r->status = FGB_SERVE_DONE;
             r->t_done = t();
             used -= r->footprint;
-            failed++;
+            completed++;
         }
-        std::vector<Request *> keep;
-        for (Request *r : live)
-            if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
-        live.swap(keep);
+        if (!done.empty()) {
+            std::vector<Request *> keep;
+            for (Request *r : live)
+                if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
+            live.swap(keep);
+        }
         cv.notify_all();
     }
 
     void run() {
         cudaSetDevice(device);
         for (;;) {
-            std::vector<Request *> next;
+            std::vector<Request *> fresh;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 cv.wait(lk, [&] { return stop || !waiting.empty() || !live.empty(); });
                 if (stop) break;
-                next = admit();
+                fresh = admit();
             }
-            if (next != batch_scenes) {
-                int rc = rebuild(next);
-                if (rc) {
-                    if (batch) fgb_batch_destroy(batch);
-                    batch = nullptr;
-                    batch_scenes.clear();
-                    fail_scenes(next, rc);
+            for (Request *r : fresh) place(r);
+            // drop empty groups, then bring the changed ones up to date
+            std::vector<std::unique_ptr<ServeGroup>> kept;
+            for (auto &g : groups) {
+                if (g->want.empty()) {
+                    if (g->batch) fgb_batch_destroy(g->batch);
                     continue;
                 }
+                kept.push_back(std::move(g));
             }
-            if (batch_scenes.empty()) continue;
-            uint64_t particles = 0;
-            for (Request *r : batch_scenes) particles += r->n;
-            const double s0 = now_s();
-            int rc = fgb_batch_step(batch, 1);
-            if (!rc) rc = fgb_batch_sync(batch);
-            const double s1 = now_s();
-            if (rc) {
-                fail_scenes(batch_scenes, rc);
-                fgb_batch_destroy(batch);
-                batch = nullptr;
-                batch_scenes.clear();
-                continue;
-            }
-            std::vector<Request *> done;
-            for (size_t k = 0; k < batch_scenes.size(); ++k) {
-                Request *r = batch_scenes[k];
-                if (--r->remaining) continue;
-                if (r->want_mesh) {
-                    rc = fgb_batch_surface(batch, (uint32_t)k, &r->mesh);
-                    if (rc) break;
-                    r->triangles = r->mesh.n;
+            groups.swap(kept);
+            for (auto &g : groups)
+                if (g->want != g->scenes) {
+                    const int rc = rebuild(*g);
+                    if (rc) fail_group(*g, rc);
                 }
-                fgb_particles v = r->view();
-                rc = fgb_batch_download(batch, (uint32_t)k, &v);
-                if (rc) break;
-                done.push_back(r);
+            // round robin over the groups that hold scenes
+            ServeGroup *pick = nullptr;
+            for (size_t i = 0; i < groups.size() && !pick; ++i) {
+                ServeGroup *g = groups[(next_group + i) % groups.size()].get();
+                if (g->batch && !g->scenes.empty()) {
+                    pick = g;
+                    next_group = (next_group + i + 1) % groups.size();
+                }
             }
-            if (rc) {
-                fail_scenes(batch_scenes, rc);
-                fgb_batch_destroy(batch);
-                batch = nullptr;
-                batch_scenes.clear();
-                continue;
-            }
-            std::lock_guard<std::mutex> lk(mu);
-            step_latency.push_back(s1 - s0);
-            busy += s1 - s0;
-            ticks++;
-            particle_steps += particles;
-            for (Request *r : done) {
-                r->status = FGB_SERVE_DONE;
-                r->t_done = t();
-                used -= r->footprint;
-                completed++;
-            }
-            if (!done.empty()) {
-                std::vector<Request *> keep;
-                for (Request *r : live)
-                    if (r->status == FGB_SERVE_ACTIVE) keep.push_back(r);
-                live.swap(keep);
-            }
-            cv.notify_all();
+            if (pick) tick(*pick);
         }
-        if (batch) fgb_batch_destroy(batch);
-        batch = nullptr;
+        for (auto &g : groups)
+            if (g->batch) fgb_batch_destroy(g->batch);
+        groups.clear();
     }
 };
 
@@ -260,6 +316,7 @@ int fgb_serve_create(fgb_solver *s, const fgb_serve_options *opt, fgb_server **o
     if (opt) sv->opt = *opt;
     if (!sv->opt.budget_bytes) sv->opt.budget_bytes = 150ull << 30;
     if (!sv->opt.max_active) sv->opt.max_active = 256;
+    if (!sv->opt.tick_particles) sv->opt.tick_particles = 2097152;
     cudaGetDevice(&sv->device);
     sv->t0 = now_s();
     sv->worker = std::thread([sv] { sv->run(); });

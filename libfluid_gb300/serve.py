@@ -10,14 +10,15 @@ class Server:
     """Continuous-batching request loop over one solver.
 
     submit() copies a scene and returns a ticket; the library's worker thread admits
-    scenes against the HBM budget, advances every resident scene one batched step
-    per tick and, when a scene has run its steps, extracts its surface (on request)
+    scenes against the HBM budget, packs resident scenes into groups of at most
+    tick_particles particles, advances one group by one batched step per tick (round
+    robin) and, when a scene has run its steps, extracts its surface (on request)
     and keeps its final state for fetch()."""
 
-    def __init__(self, solver, budget_bytes=150 << 30, max_active=256, one_at_a_time=False):
+    def __init__(self, solver, budget_bytes=150 << 30, max_active=256, one_at_a_time=False, tick_particles=0):
         self.solver = solver
         self.lib = solver.lib
-        opt = capi.ServeOptions(budget_bytes, max_active, 1 if one_at_a_time else 0)
+        opt = capi.ServeOptions(budget_bytes, max_active, 1 if one_at_a_time else 0, tick_particles)
         self._h = ctypes.c_void_p()
         capi.check(self.lib.fgb_serve_create(solver.handle, ctypes.byref(opt), ctypes.byref(self._h)))
         solver._servers.add(self)

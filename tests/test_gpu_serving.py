@@ -31,8 +31,8 @@ def _alone(solver, parts, cfg, steps, mesh):
     return got, tris
 
 
-def _serve(solver, reqs, one_at_a_time=False, stagger=0.0):
-    sv = Server(solver, budget_bytes=8 << 30, one_at_a_time=one_at_a_time)
+def _serve(solver, reqs, one_at_a_time=False, stagger=0.0, tick_particles=0):
+    sv = Server(solver, budget_bytes=8 << 30, one_at_a_time=one_at_a_time, tick_particles=tick_particles)
     tickets = []
     for parts, cfg, steps, mesh in reqs:
         tickets.append(sv.submit(cfg, parts, steps, mesh))
@@ -65,6 +65,26 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
     assert st1.ticks == sum(r[2] for r in reqs)
     for (got, tris), (got1, tris1) in zip(mixed, serial):
         assert (got["position"] == got1["position"]).all()
+    solver.close()
+
+
+def test_tick_groups_bound_the_work_per_tick_and_keep_results():
+    # 32 000 particles per tick: the 32 768-particle scene runs alone, the others
+    # share groups; every result still equals the scene advanced alone
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    reqs = _requests()
+    grouped, st, lat = _serve(solver, reqs, stagger=0.002, tick_particles=32000)
+    assert st.completed == len(reqs) and st.failed == 0
+    sizes = [len(p["mass"]) for p, _, _, _ in reqs]
+    work = sum(n * steps for n, (_, _, steps, _) in zip(sizes, reqs))
+    assert st.particle_steps == work
+    assert st.ticks >= work / max(32000, max(sizes))
+    for (parts, cfg, steps, mesh), (got, tris) in zip(reqs, grouped):
+        ref, rtris = _alone(solver, parts, cfg, steps, mesh)
+        for f in ("id", "position", "velocity", "colour"):
+            assert (got[f] == ref[f]).all(), f
+        if mesh:
+            assert len(tris) == len(rtris) and (tris == rtris).all()
     solver.close()
 
 
