@@ -76,6 +76,7 @@ struct SceneDev {
     float sphere[4];
     uint32_t n_wells, well_first;
     uint32_t tri_first, tri_count;
+    uint32_t obstacles;   // obstacle particles in the scene (0: neighbours need no type check)
     // marching cubes
     uint32_t lat[3];
     float lat_origin[3];

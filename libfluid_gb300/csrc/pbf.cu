@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(256)
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
     // fluid_known: b came from the hit list, which holds fluid particles only
     auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
-        if (!fluid_known && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+        if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(256)
         for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
             const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 <= ph.hh && __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE) hits.add(b);
+            if (r2 <= ph.hh && (!S.obstacles || __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE)) hits.add(b);
         });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(256)
     float e[3] = {0.f, 0.f, 0.f};
     // fluid_known: b came from the hit list, which holds fluid particles only
     auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
-        if (!fluid_known && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+        if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;

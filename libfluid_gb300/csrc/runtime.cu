@@ -718,6 +718,12 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     }
     b->ids[k].assign(n, 0);
     for (uint64_t i = 0; i < n; ++i) b->ids[k][i] = xs->id ? xs->id[i] : i;
+    uint32_t obstacles = 0;
+    for (uint64_t i = 0; i < n; ++i) obstacles += xs->type[i] == FGB_TYPE_OBSTACLE;
+    if (b->h_scenes[k].obstacles != obstacles) {
+        b->h_scenes[k].obstacles = obstacles;
+        b->tris_dirty = true;  // re-uploads the scene table before the next step
+    }
     const int c = b->cur;
     if (n) {
         FGB_CUDA(cudaMemcpyAsync(b->x[c].p + f, b->st_x.p, n * sizeof(float4), cudaMemcpyHostToDevice, st), "upload");
@@ -750,6 +756,10 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
     cudaStream_t st = dst->stream();
     FGB_CUDA(cudaStreamSynchronize(src->stream()), "copy_scene sync");
     const int cd = dst->cur, cs = src->cur;
+    if (dst->h_scenes[dk].obstacles != src->h_scenes[sk].obstacles) {
+        dst->h_scenes[dk].obstacles = src->h_scenes[sk].obstacles;
+        dst->tris_dirty = true;
+    }
     if (n) {
         FGB_CUDA(cudaMemcpyAsync(dst->x[cd].p + fd, src->x[cs].p + fs, n * sizeof(float4), cudaMemcpyDeviceToDevice, st),
                  "copy_scene");
