@@ -222,9 +222,13 @@ __device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint3
                                         const float4 *__restrict__ ps, F &f) {
     const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
     auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
+    // software pipeline: the next index vector is in flight while the current four
+    // candidates are loaded and processed (rows usually stream from HBM)
+    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
     uint32_t j = 0;
     for (; j + 4 <= c; j += 4) {
-        const uint4 b = load(j);
+        const uint4 b = next;
+        if (j + 4 < c) next = load(j + 4);
         const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
         f(b.x, p0);
         f(b.y, p1);
@@ -232,7 +236,7 @@ __device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint3
         f(b.w, p3);
     }
     if (j < c) {
-        const uint4 b = load(j);
+        const uint4 b = next;
         const uint32_t rest = c - j;
         const float4 p0 = __ldg(&ps[b.x]);
         const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
