@@ -90,10 +90,11 @@ __global__ void __launch_bounds__(256)
     const float thr = ph.h * S.scale;
     const float aw[3] = {node[0] * S.scale, node[1] * S.scale, node[2] * S.scale};
     float v = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
-    float cl[4] = {0.f, 0.f, 0.f, 0.f};
+    // channel sums as integers: below 2^24, so equal to the float sums in any order
+    uint32_t cl[4] = {0, 0, 0, 0};
     uint32_t N = 0;
     for_neighbour_cells(S, cells, cc[0], cc[1], cc[2], [&](uint32_t b) {
-        if (__ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
+        if (S.obstacles && __ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
         const float4 xb = __ldg(&xs[b]);
         if (PROFILE == FGB_PROFILE_REF) {
             const float lx = xb.x - aw[0], ly = xb.y - aw[1], lz = xb.z - aw[2];
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(256)
             nz = __fmaf_rn(mt, dz, nz);
         }
         const uint32_t c = __ldg(&col[b]);
-        for (int ch = 0; ch < 4; ++ch) cl[ch] += (float)argb_channel(c, ch);
+        for (int ch = 0; ch < 4; ++ch) cl[ch] += argb_channel(c, ch);
         N++;
     });
     if (PROFILE != FGB_PROFILE_REF) v = v * ph.poly6f;
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(256)
     lattice[q] = make_float4(v, nx, ny, nz);
     float avg[4] = {0.f, 0.f, 0.f, 0.f};
     if (N)
-        for (int ch = 0; ch < 4; ++ch) avg[ch] = cl[ch] / (float)N;
+        for (int ch = 0; ch < 4; ++ch) avg[ch] = (float)cl[ch] / (float)N;
     lattice_col[q] = argb_pack(avg);
 }
 

@@ -482,7 +482,8 @@ struct fgb_batch {
 
     // Grid over the current positions, then field + classify + scan for scenes [b, e).
     int surface_count(uint32_t b, uint32_t e, uint64_t *tri_total) {
-        int rc = ensure_surface();
+        int rc = sync_tris();  // the scene table (obstacle counts) as of the last upload
+        if (!rc) rc = ensure_surface();
         if (rc) return rc;
         cudaStream_t st = stream();
         StepView s = view(cur);

@@ -245,6 +245,29 @@ def test_surface_ref_profile_metaball(oracle_mod):
     solver.close()
 
 
+def test_surface_with_obstacles_and_colours_on_identical_input(oracle_mod):
+    # obstacles are left out of the field and the colour mean; the scene is surfaced
+    # straight after its upload (no step), so the obstacle count of the upload is in use
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = scenes.dam_break((14, 12, 14), (1.6, 1.6, 1.6), seed=43)
+    rng = np.random.default_rng(43)
+    parts["colour"][:] = rng.integers(0, 1 << 32, len(parts["mass"]), dtype=np.uint64).astype(np.uint32)
+    parts["type"][::7] = capi.TYPE_OBSTACLE
+    ref = scenes.copy_particles(parts)
+    solver = SphSolver(params=params)
+    batch = Batch(solver, [(parts, cfg)])
+    tris = batch.surface(0)
+    otris, olat, ocol, ocases = oracle_mod.surface(params, cfg, ref, want_lattice=True)
+    cases = batch.probe(capi.PROBE_CUBE_CASES, np.uint8)
+    assert batch.error_flags() == 0
+    assert (cases == ocases).all()
+    assert len(tris) == len(otris) > 0
+    assert np.abs(tris[:, :9] - otris[:, :9]).max() <= VERT_TOL
+    assert (tris[:, 18:].view(np.uint32) == otris[:, 18:].view(np.uint32)).all()
+    batch.close()
+    solver.close()
+
+
 def test_advance_drop_in_matches_oracle(oracle_mod):
     params = capi.params(capi.PROFILE_BASELINE, H)
     parts, cfg = scenes.dam_break((20, 20, 20), (2.0, 2.0, 2.0), seed=51)
