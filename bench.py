@@ -14,7 +14,10 @@ value      whole-job particle-steps/s, state resident in HBM, L2 flushed (a
 e2e        the same metric through fgb_advance (the reference-facing C ABI call)
            with host arrays: upload, step and write-back every step.
 roofline   the dominant kernel's algorithmic bytes per launch over its mean
-           CUDA-event duration, against the measured HBM copy bandwidth.
+           CUDA-event duration, against the measured HBM copy bandwidth; beside
+           it ("issue") the same kernel's warp instructions per launch (from the
+           committed ncu summary) over that duration, against one instruction
+           per scheduler per clock -- the ceiling the gathers meet first.
 cpu_baseline  the CPU oracle (a restatement of the reference's PBF path, OpenMP,
            every host core) on a bounded sample of the same workload.
 Multi-GPU: one single-scene replica per rank (the step does not shard without a
@@ -66,15 +69,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel, workload):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+def profiled(kernel, workload, key="dram_bytes_per_launch"):
+    """A per-launch figure of `kernel` from the committed ncu summary, or None."""
     path = os.path.join(ROOT, "profiles", f"ncu_{kernel}_{workload}.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             return float(line.split(":", 1)[1].split()[0])
     return None
+
+
+SMS, SCHEDULERS_PER_SM = 152, 4
 
 
 class Clocks:
@@ -377,7 +383,17 @@ def run_ours(args):
     algo = ALGO_BYTES[dom] * n
     achieved = algo / (mean_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic(dom, "dam_break_1m")
+    traffic = profiled(dom, "dam_break_1m")
+    # the FP32-issue ceiling of the same kernel: its warp instructions per launch
+    # (ncu) over the live launch time, against one instruction per scheduler per clock
+    inst = profiled(dom, "dam_break_1m", "warp_inst_per_launch")
+    issue = None
+    if inst:
+        mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+        ipeak = SMS * SCHEDULERS_PER_SM * mhz * 1e6
+        iach = inst / (mean_ms / 1e3)
+        issue = {"bound": "fp32-issue", "achieved": iach, "peak": ipeak, "unit": "warp-inst/s",
+                 "frac": iach / ipeak, "warp_inst_per_launch": inst, "sm_mhz": mhz}
     step_total = sum(stage_sum) / args.steps
 
     # end to end through the reference-facing call with host buffers
@@ -419,7 +435,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": algo,
-                         "mean_launch_ms": mean_ms},
+                         "mean_launch_ms": mean_ms, "issue": issue},
             "stages_ms_per_step": {nm: round(v[0] / args.steps, 4) for nm, v in per_kernel.items()},
             "stage_sum_ms_per_step": step_total,
             "cpu_baseline": cpu,
