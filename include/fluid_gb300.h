@@ -292,6 +292,36 @@ int fgb_exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_to
 int fgb_exclusive_scan_u32_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
                                    void *cuda_stream);
 
+/* ---- packed record streams (the reference demo's memory-mapped result files) --
+ * Replaces strucures::writeParticles / writeTriangles (samples/structures.hpp:
+ * 403-424) over mmf::writer::writePacked (include/fluid/mmf.hpp): a stream is a
+ * header {int64 timestamp_ms, uint64 entries, uint64 written} followed by `entries`
+ * records, every field in declaration order with no padding, little-endian:
+ *   particle (44 B): u64 id, i32 type, f32 mass, u32 colour, f32 position[3],
+ *                    f32 velocity[3]                  (structures.hpp particleDef)
+ *   triangle (84 B): f32 v0..v2[3], f32 n0..n2[3], u32 c[3]  (meshTriangleDef)
+ *   query    (32 B): u64 id, f32 point[3], u64 neighbours, u32 averageColour
+ * The header is written with written = 0, then the records, then written =
+ * entries, so a reader polling the mapped file sees a complete stream once written
+ * equals entries.  dst == NULL asks for the size only (*bytes); a capacity below it
+ * returns FGB_ERR_INVALID.  dst may be any host memory: a mapped file, a pinned
+ * buffer (fastest) or pageable memory. */
+#define FGB_WIRE_HEADER_BYTES 24
+#define FGB_WIRE_PARTICLE_BYTES 44
+#define FGB_WIRE_TRIANGLE_BYTES 84
+#define FGB_WIRE_QUERY_BYTES 32
+/* host arrays (e.g. what fgb_advance wrote back / returned) */
+int fgb_wire_particles(const fgb_particles *xs, int64_t timestamp_ms, void *dst, uint64_t capacity,
+                       uint64_t *bytes);
+int fgb_wire_triangles(const fgb_mesh *mesh, int64_t timestamp_ms, void *dst, uint64_t capacity,
+                       uint64_t *bytes);
+/* a resident scene, packed on the device and copied to dst in one transfer; the
+ * surface form streams the scene's triangles of the last fgb_batch_surface_all */
+int fgb_batch_wire_particles(fgb_batch *b, uint32_t scene, int64_t timestamp_ms, void *dst, uint64_t capacity,
+                             uint64_t *bytes);
+int fgb_batch_wire_surface(fgb_batch *b, uint32_t scene, int64_t timestamp_ms, void *dst, uint64_t capacity,
+                           uint64_t *bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -211,6 +211,13 @@ _SIGS = {
     "fgb_serve_drain": (ctypes.c_int, [c_void_p, ctypes.c_double]),
     "fgb_serve_destroy": (ctypes.c_int, [c_void_p]),
     "fgb_exclusive_scan_u32_noalloc": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p]),
+    "fgb_wire_particles": (ctypes.c_int, [P(Particles), ctypes.c_int64, c_void_p, ctypes.c_uint64,
+                                          P(ctypes.c_uint64)]),
+    "fgb_wire_triangles": (ctypes.c_int, [P(Mesh), ctypes.c_int64, c_void_p, ctypes.c_uint64, P(ctypes.c_uint64)]),
+    "fgb_batch_wire_particles": (ctypes.c_int, [c_void_p, ctypes.c_uint32, ctypes.c_int64, c_void_p,
+                                                ctypes.c_uint64, P(ctypes.c_uint64)]),
+    "fgb_batch_wire_surface": (ctypes.c_int, [c_void_p, ctypes.c_uint32, ctypes.c_int64, c_void_p,
+                                              ctypes.c_uint64, P(ctypes.c_uint64)]),
     "fgb_radix_sort_scratch_bytes": (ctypes.c_uint64, [ctypes.c_uint64]),
     "fgb_radix_sort_pairs_u32": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_uint64,
                                                 ctypes.c_uint32, c_void_p, ctypes.c_uint64, c_void_p]),

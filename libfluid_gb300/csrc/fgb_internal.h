@@ -94,6 +94,22 @@ void launch_position_keys(const StepView &s, const float4 *x, cudaStream_t st);
 void launch_gather_positions(const StepView &s, const float4 *x, const int32_t *type, const uint32_t *col,
                              float4 *xs_sorted, int32_t *type_sorted, uint32_t *col_sorted, cudaStream_t st);
 
+// Device arrays of one resident scene (current state, sorted order; the scene is
+// [first, first + n) of each array) and the triangles of its last fgb_batch_surface_all
+// (tris == nullptr before one).  Used by the record packers of wire.cu.
+struct ResidentScene {
+    uint64_t first, n;
+    const float4 *x, *v;
+    const int32_t *type;
+    const uint32_t *col, *slot;
+    const uint64_t *ids;  // by upload slot, indexed first + slot
+    cudaStream_t stream;
+    const fgb_mesh_triangle *tris;
+    uint64_t tri_count;
+};
+int batch_resident(fgb_batch *b, uint32_t scene, ResidentScene *out);
+void *batch_wire_scratch(fgb_batch *b, uint64_t bytes);  // device staging, grown on demand
+
 // marching cubes (mc.cu)
 struct SurfaceView {
     const SceneDev *scenes;   // device

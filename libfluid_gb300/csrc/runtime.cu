@@ -217,6 +217,8 @@ struct fgb_batch {
     Dev<float4> x[2], v[2];
     Dev<int32_t> type[2];
     Dev<uint32_t> col[2], slot[2];
+    Dev<uint64_t> ids_dev;  // particle ids by upload slot (scene segment), for device-side record packing
+    Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
     Dev<uint32_t> keys_in, vals_in, keys_sorted, vals_sorted;
@@ -633,6 +635,7 @@ static int batch_init(fgb_batch *b) {
         FGB_CUDA(b->type[c].alloc(n), "batch alloc");
         FGB_CUDA(b->col[c].alloc(n), "batch alloc");
         FGB_CUDA(b->slot[c].alloc(n), "batch alloc");
+        if (c == 0) FGB_CUDA(b->ids_dev.alloc(n), "batch alloc");
         FGB_CUDA(b->ps[c].alloc(n), "batch alloc");
     }
     FGB_CUDA(b->keys_in.alloc(n), "batch alloc");
@@ -719,6 +722,10 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     }
     b->ids[k].assign(n, 0);
     for (uint64_t i = 0; i < n; ++i) b->ids[k][i] = xs->id ? xs->id[i] : i;
+    if (n)
+        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + f, b->ids[k].data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                 b->stream()),
+                 "upload ids");
     uint32_t obstacles = 0;
     for (uint64_t i = 0; i < n; ++i) obstacles += xs->type[i] == FGB_TYPE_OBSTACLE;
     if (b->h_scenes[k].obstacles != obstacles) {
@@ -773,6 +780,9 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
                                  cudaMemcpyDeviceToDevice, st),
                  "copy_scene");
         FGB_CUDA(cudaMemcpyAsync(dst->slot[cd].p + fd, src->slot[cs].p + fs, n * sizeof(uint32_t),
+                                 cudaMemcpyDeviceToDevice, st),
+                 "copy_scene");
+        FGB_CUDA(cudaMemcpyAsync(dst->ids_dev.p + fd, src->ids_dev.p + fs, n * sizeof(uint64_t),
                                  cudaMemcpyDeviceToDevice, st),
                  "copy_scene");
         launch_fill_u32(dst->keys_sorted.p + fd, n, dst->mbits >= 32 ? 0u : (dk << dst->mbits), st);
@@ -1099,6 +1109,36 @@ int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts) {
         if (counts) counts[k] = b->surf_tri_first[k + 1] - b->surf_tri_first[k];
     return FGB_OK;
 }
+
+extern "C++" {
+namespace fgb {
+int batch_resident(fgb_batch *b, uint32_t k, ResidentScene *out) {
+    if (!b || !out || k >= b->n_scenes) return fail(FGB_ERR_INVALID, "resident scene: bad argument");
+    const int c = b->cur;
+    out->first = b->first[k];
+    out->n = b->counts[k];
+    out->x = b->x[c].p;
+    out->v = b->v[c].p;
+    out->type = b->type[c].p;
+    out->col = b->col[c].p;
+    out->slot = b->slot[c].p;
+    out->ids = b->ids_dev.p;
+    out->stream = b->stream();
+    out->tris = nullptr;
+    out->tri_count = 0;
+    if (b->surf_tri_first.size() == b->n_scenes + 1) {
+        out->tris = b->tris_out.p + b->surf_tri_first[k];
+        out->tri_count = b->surf_tri_first[k + 1] - b->surf_tri_first[k];
+    }
+    return FGB_OK;
+}
+
+void *batch_wire_scratch(fgb_batch *b, uint64_t bytes) {
+    if (b->wire.n < bytes && b->wire.alloc(bytes) != cudaSuccess) return nullptr;
+    return b->wire.p;
+}
+}  // namespace fgb
+}  // extern "C++"
 
 int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out) {
     if (!b || scene >= b->n_scenes || b->surf_tri_first.size() != b->n_scenes + 1)

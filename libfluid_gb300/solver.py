@@ -112,6 +112,10 @@ class Batch:
         tp = tris.ctypes.data_as(_P(capi.Triangle)) if tris is not None else None
         capi.check(self.lib.fgb_batch_set_colliders(self._h, k, tp, ntris))
 
+    @property
+    def handle(self):
+        return self._h
+
     def step(self, steps=1):
         capi.check(self.lib.fgb_batch_step(self._h, steps))
 
