@@ -322,6 +322,18 @@ int fgb_batch_wire_particles(fgb_batch *b, uint32_t scene, int64_t timestamp_ms,
 int fgb_batch_wire_surface(fgb_batch *b, uint32_t scene, int64_t timestamp_ms, void *dst, uint64_t capacity,
                            uint64_t *bytes);
 
+/* ---- vertex welding: an index buffer for a triangle soup -------------------
+ * geometry::indexVBO2 (include/fluid/geometry.hpp:152-166): the vertices v0, v1,
+ * v2 of each triangle in order; a position byte-identical to an earlier one reuses
+ * its index, otherwise it is appended.  Output: indices[3 n] (32-bit; the
+ * reference's unsigned short wraps after 65 535 vertices) and the distinct
+ * positions in order of first appearance, vertices[3 * *n_vertices] (room for 9 n
+ * floats must be given).  Computed on the device; the result is the sequential
+ * one exactly.  The batch form welds the scene's triangles of the last
+ * fgb_batch_surface_all where they lie. */
+int fgb_weld_mesh(const fgb_mesh *mesh, uint32_t *indices, float *vertices, uint64_t *n_vertices);
+int fgb_batch_weld_surface(fgb_batch *b, uint32_t scene, uint32_t *indices, float *vertices, uint64_t *n_vertices);
+
 #ifdef __cplusplus
 }
 #endif

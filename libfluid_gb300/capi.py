@@ -1,8 +1,8 @@
 """ctypes view of the C ABI declared in include/fluid_gb300.h.
 
-The structs here mirror the header field by field; `tests/test_capi_layout.py`
-checks their sizes and offsets against the compiled library's own `sizeof`
-report so that a drift between the two fails loudly.
+The structs here mirror the header field by field; `tests/test_capi_cpu.py`
+checks their sizes against the compiled library's own `sizeof` report so that a
+drift between the two fails loudly.
 """
 import ctypes
 import os
@@ -218,6 +218,8 @@ _SIGS = {
                                                 ctypes.c_uint64, P(ctypes.c_uint64)]),
     "fgb_batch_wire_surface": (ctypes.c_int, [c_void_p, ctypes.c_uint32, ctypes.c_int64, c_void_p,
                                               ctypes.c_uint64, P(ctypes.c_uint64)]),
+    "fgb_weld_mesh": (ctypes.c_int, [P(Mesh), c_void_p, c_void_p, P(ctypes.c_uint64)]),
+    "fgb_batch_weld_surface": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, c_void_p, P(ctypes.c_uint64)]),
     "fgb_radix_sort_scratch_bytes": (ctypes.c_uint64, [ctypes.c_uint64]),
     "fgb_radix_sort_pairs_u32": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_uint64,
                                                 ctypes.c_uint32, c_void_p, ctypes.c_uint64, c_void_p]),

@@ -16,6 +16,7 @@ enum : uint32_t {
     ERR_SCAN_LOOKBACK = 1u << 1,  // prefix-scan look-back wait gave up
     ERR_CELL_RANGE = 1u << 2,     // a key outside its scene's cell table
     ERR_MESH_CAPACITY = 1u << 3,  // more triangles than the output buffer holds
+    ERR_WELD_TABLE = 1u << 4,     // a vertex found no slot in the welding hash table
 };
 
 // Bound on every look-back spin: after this many polls the waiting CTA records an

@@ -110,6 +110,10 @@ struct ResidentScene {
 int batch_resident(fgb_batch *b, uint32_t scene, ResidentScene *out);
 void *batch_wire_scratch(fgb_batch *b, uint64_t bytes);  // device staging, grown on demand
 
+// vertex welding of device-resident triangles (weld.cu)
+int weld_device(const fgb_mesh_triangle *d_tris, uint64_t n_tris, uint32_t *d_index, float *d_vertices,
+                uint64_t *n_vertices, cudaStream_t st);
+
 // marching cubes (mc.cu)
 struct SurfaceView {
     const SceneDev *scenes;   // device

@@ -54,6 +54,8 @@ def lib():
                                   vp, vp, vp, ctypes.c_size_t]
         L.orc_march.restype = ctypes.c_size_t
         L.orc_march.argtypes = [P(capi.Params), P(capi.Config), vp, vp, vp, vp, vp, ctypes.c_size_t]
+        L.orc_weld.restype = ctypes.c_size_t
+        L.orc_weld.argtypes = [vp, ctypes.c_size_t, vp, vp]
         L.orc_num_threads.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
         _lib = L
@@ -185,6 +187,16 @@ def march(params, cfg, lat, lcol):
     L.orc_march(ctypes.byref(params), ctypes.byref(cfg), ctypes.byref(l), _ptr(lat), _ptr(lcol), None,
                 _ptr(tris), total)
     return tris[:total], cases[:cubes]
+
+
+def weld(tris):
+    """(indices, vertices) of an (n, 21) float32 triangle array (geometry.hpp:152-166)."""
+    tris = np.ascontiguousarray(tris, np.float32)
+    n = len(tris)
+    idx = np.zeros(3 * n, np.uint32)
+    verts = np.zeros(9 * n, np.float32)
+    m = lib().orc_weld(_ptr(tris), n, _ptr(idx), _ptr(verts)) if n else 0
+    return idx, verts[:3 * m].reshape(-1, 3)
 
 
 def set_threads(n):

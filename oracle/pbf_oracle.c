@@ -1037,3 +1037,51 @@ size_t orc_surface(const fgb_params *p, const fgb_config *c, size_t n, const int
     free(cells);
     return total;
 }
+
+/* ------------------------------------------------------------ vertex welding */
+
+typedef struct weld_item {
+    uint32_t key[3];
+    uint32_t idx;
+} weld_item;
+
+static int cmp_weld(const void *a, const void *b) {
+    const weld_item *x = (const weld_item *)a, *y = (const weld_item *)b;
+    for (int k = 0; k < 3; ++k)
+        if (x->key[k] != y->key[k]) return x->key[k] < y->key[k] ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+/* geometry.hpp:152-166 (first appearance wins), by sorting (position bytes, index):
+ * within a run of equal positions the first item holds the smallest index. */
+size_t orc_weld(const fgb_mesh_triangle *tris, size_t n, uint32_t *indices, float *vertices) {
+    const size_t nv = 3 * n;
+    if (!nv) return 0;
+    weld_item *it = (weld_item *)malloc(nv * sizeof(weld_item));
+    uint32_t *first = (uint32_t *)malloc(nv * sizeof(uint32_t));
+    uint32_t *rank = (uint32_t *)malloc(nv * sizeof(uint32_t));
+    for (size_t i = 0; i < nv; ++i) {
+        memcpy(it[i].key, &tris[i / 3].v[3 * (i % 3)], 12);
+        it[i].idx = (uint32_t)i;
+    }
+    qsort(it, nv, sizeof(weld_item), cmp_weld);
+    for (size_t s = 0; s < nv;) {
+        size_t e = s + 1;
+        while (e < nv && memcmp(it[e].key, it[s].key, 12) == 0) ++e;
+        for (size_t j = s; j < e; ++j) first[it[j].idx] = it[s].idx;
+        s = e;
+    }
+    size_t count = 0;
+    for (size_t i = 0; i < nv; ++i) {
+        if (first[i] == (uint32_t)i) {
+            rank[i] = (uint32_t)count;
+            memcpy(&vertices[3 * count], &tris[i / 3].v[3 * (i % 3)], 12);
+            ++count;
+        }
+        indices[i] = rank[first[i]];
+    }
+    free(it);
+    free(first);
+    free(rank);
+    return count;
+}

@@ -80,6 +80,12 @@ size_t orc_march(const fgb_params *p, const fgb_config *c, const orc_lattice *l,
                  const float *lattice, const uint32_t *lattice_colour, uint8_t *cases,
                  fgb_mesh_triangle *tris, size_t cap);
 
+/* Vertex welding (geometry::indexVBO2, geometry.hpp:152-166): the vertices of the
+ * triangles in order; a position byte-identical to an earlier one takes its index,
+ * otherwise it is appended.  indices: 3 n; vertices: room for 9 n floats.  Returns
+ * the number of distinct vertices. */
+size_t orc_weld(const fgb_mesh_triangle *tris, size_t n, uint32_t *indices, float *vertices);
+
 int orc_num_threads(void);
 void orc_set_threads(int n);
 
