@@ -124,7 +124,8 @@ int fgb_version(void);
 /* Message of the last failure on this thread ("" when none). */
 const char *fgb_last_error(void);
 /* sizeof of the ABI structs in this order: fgb_params, fgb_config, fgb_particles,
- * fgb_triangle, fgb_mesh_triangle, fgb_mesh, fgb_grid_info, fgb_well; writes at most
+ * fgb_triangle, fgb_mesh_triangle, fgb_mesh, fgb_grid_info, fgb_well,
+ * fgb_serve_options, fgb_serve_result, fgb_serve_stats, fgb_tune_result; writes at most
  * n values and returns how many exist.  Replaces the reference's check_size kernel
  * and host assert of struct layouts (oclsph_kernel.h:276-278, oclsph.hpp:217-243). */
 int fgb_struct_sizes(uint64_t *out, int n);
@@ -176,6 +177,21 @@ uint64_t fgb_batch_launch_count(const fgb_batch *b);
  * (predict, sort, reorder, lambda/delta per iteration, vorticity, vorticity apply);
  * fgb_batch_stage_times returns the last step's per-stage milliseconds. */
 int fgb_batch_set_timing(fgb_batch *b, int on);
+/* Autotuner: runs the batch's next steps under each candidate launch shape (gather
+ * CTA size 64, 128, 256 at the current Verlet skin, then skins 0.1-0.3 h at the best
+ * size; steps_per_trial steps each, the first untimed), keeps the fastest, and caches
+ * it in the solver for every later batch of the same physics profile and size
+ * bucket (floor(log2(particles))).  The trial steps are ordinary steps: no knob
+ * changes a result, so a tuned batch computes the same bits as an untuned one.
+ * No counterpart in the reference (work-group sizes are left to the OpenCL
+ * runtime, oclsph.hpp:597). */
+typedef struct fgb_tune_result {
+    uint32_t block;      /* threads per CTA of the gather kernels */
+    float skin;          /* Verlet skin, in units of h */
+    float ms_per_step;   /* of the chosen shape */
+    uint32_t trials, steps;
+} fgb_tune_result;
+int fgb_batch_autotune(fgb_batch *b, uint32_t steps_per_trial, fgb_tune_result *out);
 int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count);
 
 /* Parity probes: copy an internal array of the last step to host memory.

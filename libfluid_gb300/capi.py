@@ -167,6 +167,11 @@ class ServeStats(ctypes.Structure):
     ]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_uint32), ("skin", ctypes.c_float), ("ms_per_step", ctypes.c_float),
+                ("trials", ctypes.c_uint32), ("steps", ctypes.c_uint32)]
+
+
 P = ctypes.POINTER
 c_void_p = ctypes.c_void_p
 
@@ -194,6 +199,7 @@ _SIGS = {
     "fgb_batch_error_flags": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),
     "fgb_batch_set_timing": (ctypes.c_int, [c_void_p, ctypes.c_int]),
+    "fgb_batch_autotune": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(TuneResult)]),
     "fgb_batch_stage_times": (ctypes.c_int, [c_void_p, P(ctypes.c_float), ctypes.c_uint32, P(ctypes.c_uint32)]),
     "fgb_batch_probe_size": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(ctypes.c_uint64)]),
     "fgb_batch_probe": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, ctypes.c_uint64]),

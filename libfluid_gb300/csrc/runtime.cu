@@ -22,6 +22,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "fgb_internal.h"
@@ -185,6 +186,13 @@ void ensure_tables() {
 
 using namespace fgb;
 
+// Autotuner cache key: physics profile and floor(log2(particles)).
+static uint32_t tune_bucket(int32_t profile, uint64_t n) {
+    uint32_t b = 0;
+    while (b < 63 && (2ull << b) <= n) ++b;
+    return (uint32_t)profile * 64u + b;
+}
+
 struct fgb_solver {
     fgb_params params;
     Phys ph;
@@ -192,6 +200,12 @@ struct fgb_solver {
     cudaStream_t stream = nullptr;
     int device = 0;
     int block = 128;
+    // autotuned launch shape per (profile, log2 particle count) bucket
+    struct Tuned {
+        int block;
+        float skin;
+    };
+    std::map<uint32_t, Tuned> tuned;
     fgb_batch *cached = nullptr;  // single-scene batch behind fgb_advance
     uint64_t cached_n = 0;
     fgb_config cached_cfg{};
@@ -238,6 +252,7 @@ struct fgb_batch {
     uint32_t hit_cap = 64;
     uint32_t list_cap = 96;
     float skin_frac = 0.2f;
+    int block = 128;  // threads per CTA of the gather kernels
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
     Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
@@ -310,7 +325,7 @@ struct fgb_batch {
         s.omega = omega.p;
         s.vx = vx.p;
         s.err = err.p;
-        s.block = solver->block;
+        s.block = block;
         s.nlist = nlist.p;
         s.ncount = ncount.p;
         s.cap = nlist.p ? list_cap : 0;
@@ -383,6 +398,67 @@ struct fgb_batch {
         FGB_CUDA(cudaGetLastError(), "step: launch");
         launches_per_step = l;
         if (timing) n_stages = k ? k - 1 : 0;
+        return FGB_OK;
+    }
+
+    // Time `per_trial` - 1 steps (after one untimed step) under each candidate
+    // launch shape: CTA sizes first at the current skin, then skins at the best CTA
+    // size.  Neither knob changes a result (the lists are exact for any skin, and
+    // each thread owns one particle), so these are ordinary steps of the batch.
+    int autotune(uint32_t per_trial, fgb_tune_result *out) {
+        if (per_trial < 2) per_trial = 2;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        FGB_CUDA(cudaEventCreate(&e0), "autotune event");
+        FGB_CUDA(cudaEventCreate(&e1), "autotune event");
+        uint32_t trials = 0, steps = 0;
+        auto trial = [&](int blk, float skin, float *ms) -> int {
+            block = blk;
+            skin_frac = skin;
+            for (auto &g : graph)
+                if (g) cudaGraphExecDestroy(g), g = nullptr;
+            graphs_ok = false;
+            int rc = step(1);
+            if (!rc) rc = cudaEventRecord(e0, stream()) == cudaSuccess ? FGB_OK : fail(FGB_ERR_CUDA, "autotune");
+            if (!rc) rc = step(per_trial - 1);
+            if (!rc) rc = cudaEventRecord(e1, stream()) == cudaSuccess ? FGB_OK : fail(FGB_ERR_CUDA, "autotune");
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(FGB_ERR_CUDA, "autotune sync");
+            float t = 0.f;
+            if (!rc) cudaEventElapsedTime(&t, e0, e1);
+            *ms = t / (float)(per_trial - 1);
+            trials++;
+            steps += per_trial;
+            return rc;
+        };
+        int rc = FGB_OK;
+        int best_block = block;
+        float best_skin = skin_frac, best_ms = 3.4e38f, ms = 0.f;
+        const float skin0 = skin_frac;
+        for (int blk : {64, 128, 256}) {
+            rc = trial(blk, skin0, &ms);
+            if (rc) break;
+            if (ms < best_ms) best_ms = ms, best_block = blk;
+        }
+        for (float skin : {0.1f, 0.15f, 0.25f, 0.3f}) {
+            if (rc || skin == skin0) continue;
+            rc = trial(best_block, skin, &ms);
+            if (!rc && ms < best_ms) best_ms = ms, best_skin = skin;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        block = best_block;
+        skin_frac = best_skin;
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        graphs_ok = false;
+        if (rc) return rc;
+        solver->tuned[tune_bucket(solver->params.profile, n)] = {best_block, best_skin};
+        if (out) {
+            out->block = (uint32_t)best_block;
+            out->skin = best_skin;
+            out->ms_per_step = best_ms;
+            out->trials = trials;
+            out->steps = steps;
+        }
         return FGB_OK;
     }
 
@@ -647,6 +723,14 @@ static int batch_init(fgb_batch *b) {
     FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
     FGB_CUDA(b->ps_grid.alloc(n), "batch alloc");
     if (const char *e = getenv("FGB_LIST_CAP")) b->list_cap = (uint32_t)atoi(e);
+    b->block = s->block;
+    {
+        auto it = s->tuned.find(tune_bucket(p.profile, n));
+        if (it != s->tuned.end()) {
+            b->block = it->second.block;
+            b->skin_frac = it->second.skin;
+        }
+    }
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
@@ -904,7 +988,7 @@ int fgb_struct_sizes(uint64_t *out, int n) {
     const uint64_t sizes[] = {sizeof(fgb_params), sizeof(fgb_config),        sizeof(fgb_particles),
                               sizeof(fgb_triangle), sizeof(fgb_mesh_triangle), sizeof(fgb_mesh),
                               sizeof(fgb_grid_info), sizeof(fgb_well),          sizeof(fgb_serve_options),
-                              sizeof(fgb_serve_result), sizeof(fgb_serve_stats)};
+                              sizeof(fgb_serve_result), sizeof(fgb_serve_stats), sizeof(fgb_tune_result)};
     const int m = (int)(sizeof(sizes) / sizeof(sizes[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = sizes[i];
     return m;
@@ -1163,6 +1247,12 @@ int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
 }
 
 uint64_t fgb_batch_launch_count(const fgb_batch *b) { return b ? b->launches : 0; }
+
+int fgb_batch_autotune(fgb_batch *b, uint32_t steps_per_trial, fgb_tune_result *out) {
+    if (!b) return fail(FGB_ERR_INVALID, "autotune: null batch");
+    if (b->n == 0) return FGB_OK;
+    return b->autotune(steps_per_trial, out);
+}
 
 int fgb_batch_set_timing(fgb_batch *b, int on) {
     if (!b) return fail(FGB_ERR_INVALID, "set_timing: null batch");

@@ -122,6 +122,13 @@ class Batch:
     def sync(self):
         capi.check(self.lib.fgb_batch_sync(self._h))
 
+    def autotune(self, steps_per_trial=3):
+        """Pick the fastest launch shape on this batch's next steps (they are ordinary
+        steps) and cache it in the solver for its size bucket; returns TuneResult."""
+        r = capi.TuneResult()
+        capi.check(self.lib.fgb_batch_autotune(self._h, steps_per_trial, ctypes.byref(r)))
+        return r
+
     def download(self, k):
         n = self.counts[k]
         out = {
