@@ -20,7 +20,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <map>
 #include <vector>
@@ -185,6 +187,28 @@ void ensure_tables() {
 }  // namespace fgb
 
 using namespace fgb;
+
+// Run f(lo, hi) over [0, n) on up to one host thread per core, in chunks of at
+// least 64k items (the per-frame pack/unpack loops of upload and download).
+template <class F>
+static void parallel_for(uint64_t n, F &&f) {
+    const uint64_t min_chunk = 1u << 16;
+    uint64_t t = std::max(1u, std::thread::hardware_concurrency());
+    t = std::min<uint64_t>(t, (n + min_chunk - 1) / min_chunk);
+    if (t <= 1) {
+        f((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(t - 1);
+    const uint64_t chunk = (n + t - 1) / t;
+    for (uint64_t i = 1; i < t; ++i) {
+        const uint64_t lo = i * chunk, hi = std::min(n, lo + chunk);
+        if (lo < hi) pool.emplace_back([&f, lo, hi] { f(lo, hi); });
+    }
+    f((uint64_t)0, std::min(n, chunk));
+    for (auto &th : pool) th.join();
+}
 
 // Autotuner cache key: physics profile and floor(log2(particles)).
 static uint32_t tune_bucket(int32_t profile, uint64_t n) {
@@ -797,21 +821,27 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     FGB_CUDA(b->st_slot.ensure(n), "upload staging");
     cudaStream_t st = b->stream();
     FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
-    for (uint64_t i = 0; i < n; ++i) {
-        b->st_x.p[i] = make_float4(xs->position[3 * i], xs->position[3 * i + 1], xs->position[3 * i + 2], xs->mass[i]);
-        b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
-        b->st_type.p[i] = xs->type[i];
-        b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
-        b->st_slot.p[i] = (uint32_t)i;
-    }
-    b->ids[k].assign(n, 0);
-    for (uint64_t i = 0; i < n; ++i) b->ids[k][i] = xs->id ? xs->id[i] : i;
+    b->ids[k].resize(n);
+    std::atomic<uint32_t> obstacle_count{0};
+    uint64_t *ids = b->ids[k].data();
+    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
+        uint32_t obst = 0;
+        for (uint64_t i = lo; i < hi; ++i) {
+            b->st_x.p[i] =
+                make_float4(xs->position[3 * i], xs->position[3 * i + 1], xs->position[3 * i + 2], xs->mass[i]);
+            b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
+            b->st_type.p[i] = xs->type[i];
+            b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
+            b->st_slot.p[i] = (uint32_t)i;
+            ids[i] = xs->id ? xs->id[i] : i;
+            obst += xs->type[i] == FGB_TYPE_OBSTACLE;
+        }
+        obstacle_count += obst;
+    });
     if (n)
-        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + f, b->ids[k].data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                                 b->stream()),
+        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + f, ids, n * sizeof(uint64_t), cudaMemcpyHostToDevice, b->stream()),
                  "upload ids");
-    uint32_t obstacles = 0;
-    for (uint64_t i = 0; i < n; ++i) obstacles += xs->type[i] == FGB_TYPE_OBSTACLE;
+    const uint32_t obstacles = obstacle_count.load();
     if (b->h_scenes[k].obstacles != obstacles) {
         b->h_scenes[k].obstacles = obstacles;
         b->tris_dirty = true;  // re-uploads the scene table before the next step
@@ -828,11 +858,7 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
                  "upload");
     }
     // the scene's key prefix, in case a surface call precedes the first step
-    FGB_CUDA(b->st_keys.ensure(n), "upload staging");
-    for (uint64_t i = 0; i < n; ++i) b->st_keys.p[i] = b->mbits >= 32 ? 0u : (k << b->mbits);
-    if (n)
-        FGB_CUDA(cudaMemcpyAsync(b->keys_sorted.p + f, b->st_keys.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
-                 "upload");
+    launch_fill_u32(b->keys_sorted.p + f, n, b->mbits >= 32 ? 0u : (k << b->mbits), st);
     FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
     return FGB_OK;
 }
@@ -925,24 +951,26 @@ static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
     }
     FGB_CUDA(cudaStreamSynchronize(st), "download sync");
     const std::vector<uint64_t> &ids = b->ids[k];
-    for (uint64_t i = 0; i < n; ++i) {
-        const float4 X = b->st_x.p[i], V = b->st_v.p[i];
-        if (xs->position) {
-            xs->position[3 * i] = X.x;
-            xs->position[3 * i + 1] = X.y;
-            xs->position[3 * i + 2] = X.z;
+    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            const float4 X = b->st_x.p[i], V = b->st_v.p[i];
+            if (xs->position) {
+                xs->position[3 * i] = X.x;
+                xs->position[3 * i + 1] = X.y;
+                xs->position[3 * i + 2] = X.z;
+            }
+            if (xs->mass) xs->mass[i] = X.w;
+            if (xs->velocity) {
+                xs->velocity[3 * i] = V.x;
+                xs->velocity[3 * i + 1] = V.y;
+                xs->velocity[3 * i + 2] = V.z;
+            }
+            if (xs->type) xs->type[i] = b->st_type.p[i];
+            if (xs->colour) xs->colour[i] = b->st_col.p[i];
+            const uint32_t sl = b->st_slot.p[i];
+            if (xs->id) xs->id[i] = sl < ids.size() ? ids[sl] : sl;
         }
-        if (xs->mass) xs->mass[i] = X.w;
-        if (xs->velocity) {
-            xs->velocity[3 * i] = V.x;
-            xs->velocity[3 * i + 1] = V.y;
-            xs->velocity[3 * i + 2] = V.z;
-        }
-        if (xs->type) xs->type[i] = b->st_type.p[i];
-        if (xs->colour) xs->colour[i] = b->st_col.p[i];
-        const uint32_t sl = b->st_slot.p[i];
-        if (xs->id) xs->id[i] = sl < ids.size() ? ids[sl] : sl;
-    }
+    });
     return FGB_OK;
 }
 
