@@ -21,10 +21,13 @@
 #include <cstdio>
 #include <cstring>
 #include <atomic>
+#include <condition_variable>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <string>
 #include <map>
+#include <memory>
 #include <vector>
 
 #include "fgb_internal.h"
@@ -188,27 +191,104 @@ void ensure_tables() {
 
 using namespace fgb;
 
-// Run f(lo, hi) over [0, n) on up to one host thread per core, in chunks of at
-// least 64k items (the per-frame pack/unpack loops of upload and download).
+// Host worker pool for the per-frame pack and unpack loops of upload and download:
+// one thread per core, started on first use and parked on a condition variable
+// between jobs; the calling thread works too.  A job is f(lo, hi) over [0, n),
+// handed out in chunks of 16k items.  Jobs from different threads are serialised.
+class HostPool {
+  public:
+    static HostPool &get() {
+        static HostPool pool;
+        return pool;
+    }
+    template <class F>
+    void run(uint64_t n, F &&f) {
+        const uint64_t chunks = (n + kChunk - 1) / kChunk;
+        if (chunks <= 1 || workers_.empty()) {
+            if (n) f((uint64_t)0, n);
+            return;
+        }
+        std::lock_guard<std::mutex> job_lock(job_mu_);
+        auto job = std::make_shared<Job>();
+        job->f = [&f](uint64_t lo, uint64_t hi) { f(lo, hi); };
+        job->n = n;
+        job->chunks = chunks;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            current_ = job;
+            ++generation_;
+        }
+        cv_.notify_all();
+        work(*job);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return job->done.load() == job->chunks; });
+        current_.reset();
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+            ++generation_;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+
+  private:
+    static constexpr uint64_t kChunk = 1u << 14;
+    // One job's state: a worker that wakes late finds every chunk taken and leaves,
+    // and run() returns only once every taken chunk has finished.
+    struct Job {
+        std::function<void(uint64_t, uint64_t)> f;
+        uint64_t n = 0, chunks = 0;
+        std::atomic<uint64_t> next{0}, done{0};
+    };
+    HostPool() {
+        const unsigned t = std::max(1u, std::thread::hardware_concurrency());
+        for (unsigned i = 1; i < t; ++i) workers_.emplace_back([this] { loop(); });
+    }
+    void work(Job &j) {
+        for (;;) {
+            const uint64_t c = j.next.fetch_add(1);
+            if (c >= j.chunks) return;
+            j.f(c * kChunk, std::min(j.n, (c + 1) * kChunk));
+            if (j.done.fetch_add(1) + 1 == j.chunks) {
+                std::lock_guard<std::mutex> lk(mu_);
+                done_cv_.notify_all();
+            }
+        }
+    }
+    void loop() {
+        uint64_t seen = 0;
+        for (;;) {
+            std::shared_ptr<Job> job;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || generation_ != seen; });
+                if (stop_) return;
+                seen = generation_;
+                job = current_;
+            }
+            if (job) work(*job);
+        }
+    }
+    std::vector<std::thread> workers_;
+    std::mutex job_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    std::shared_ptr<Job> current_;
+    uint64_t generation_ = 0;
+    bool stop_ = false;
+};
+
 template <class F>
 static void parallel_for(uint64_t n, F &&f) {
-    const uint64_t min_chunk = 1u << 16;
-    uint64_t t = std::max(1u, std::thread::hardware_concurrency());
-    t = std::min<uint64_t>(t, (n + min_chunk - 1) / min_chunk);
-    if (t <= 1) {
-        f((uint64_t)0, n);
-        return;
-    }
-    std::vector<std::thread> pool;
-    pool.reserve(t - 1);
-    const uint64_t chunk = (n + t - 1) / t;
-    for (uint64_t i = 1; i < t; ++i) {
-        const uint64_t lo = i * chunk, hi = std::min(n, lo + chunk);
-        if (lo < hi) pool.emplace_back([&f, lo, hi] { f(lo, hi); });
-    }
-    f((uint64_t)0, std::min(n, chunk));
-    for (auto &th : pool) th.join();
+    HostPool::get().run(n, f);
 }
+
+// Pieces of the pipelined upload and download: host packing or unpacking of one
+// piece overlaps the copies of the others.
+static constexpr uint64_t kPieceMin = 1u << 18;
+static constexpr uint32_t kPieces = 4;
 
 // Autotuner cache key: physics profile and floor(log2(particles)).
 static uint32_t tune_bucket(int32_t profile, uint64_t n) {
@@ -304,6 +384,8 @@ struct fgb_batch {
     Pinned<float4> st_x, st_v;
     Pinned<int32_t> st_type;
     Pinned<uint32_t> st_col, st_slot, st_keys;
+    Pinned<uint64_t> st_ids;
+    std::vector<cudaEvent_t> piece_events;  // pipelined download, one per piece
     uint64_t launches = 0;
     uint64_t launches_per_step = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -313,6 +395,7 @@ struct fgb_batch {
         for (auto &g : graph)
             if (g) cudaGraphExecDestroy(g);
         for (auto &ev : events) cudaEventDestroy(ev);
+        for (auto &ev : piece_events) cudaEventDestroy(ev);
     }
 
     cudaStream_t stream() const { return solver->stream; }
@@ -821,45 +904,55 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     FGB_CUDA(b->st_slot.ensure(n), "upload staging");
     cudaStream_t st = b->stream();
     FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
+    FGB_CUDA(b->st_ids.ensure(n), "upload staging");
     b->ids[k].resize(n);
     std::atomic<uint32_t> obstacle_count{0};
     uint64_t *ids = b->ids[k].data();
-    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
-        uint32_t obst = 0;
-        for (uint64_t i = lo; i < hi; ++i) {
-            b->st_x.p[i] =
-                make_float4(xs->position[3 * i], xs->position[3 * i + 1], xs->position[3 * i + 2], xs->mass[i]);
-            b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
-            b->st_type.p[i] = xs->type[i];
-            b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
-            b->st_slot.p[i] = (uint32_t)i;
-            ids[i] = xs->id ? xs->id[i] : i;
-            obst += xs->type[i] == FGB_TYPE_OBSTACLE;
-        }
-        obstacle_count += obst;
-    });
-    if (n)
-        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + f, ids, n * sizeof(uint64_t), cudaMemcpyHostToDevice, b->stream()),
+    const int c = b->cur;
+    // piece by piece: pack on the host threads, then queue the piece's copies, which
+    // run while the next piece is packed
+    const uint64_t piece = std::max<uint64_t>(kPieceMin, (n + kPieces - 1) / kPieces);
+    for (uint64_t p0 = 0; p0 < n; p0 += piece) {
+        const uint64_t m = std::min(n - p0, piece);
+        parallel_for(m, [&](uint64_t lo, uint64_t hi) {
+            uint32_t obst = 0;
+            for (uint64_t i = p0 + lo; i < p0 + hi; ++i) {
+                b->st_x.p[i] =
+                    make_float4(xs->position[3 * i], xs->position[3 * i + 1], xs->position[3 * i + 2], xs->mass[i]);
+                b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
+                b->st_type.p[i] = xs->type[i];
+                b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
+                b->st_slot.p[i] = (uint32_t)i;
+                ids[i] = b->st_ids.p[i] = xs->id ? xs->id[i] : i;
+                obst += xs->type[i] == FGB_TYPE_OBSTACLE;
+            }
+            obstacle_count += obst;
+        });
+        const uint64_t d = f + p0;
+        FGB_CUDA(cudaMemcpyAsync(b->x[c].p + d, b->st_x.p + p0, m * sizeof(float4), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->v[c].p + d, b->st_v.p + p0, m * sizeof(float4), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->type[c].p + d, b->st_type.p + p0, m * sizeof(int32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->col[c].p + d, b->st_col.p + p0, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->slot[c].p + d, b->st_slot.p + p0, m * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 st),
+                 "upload");
+        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + d, b->st_ids.p + p0, m * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                 st),
                  "upload ids");
+    }
     const uint32_t obstacles = obstacle_count.load();
     if (b->h_scenes[k].obstacles != obstacles) {
         b->h_scenes[k].obstacles = obstacles;
         b->tris_dirty = true;  // re-uploads the scene table before the next step
     }
-    const int c = b->cur;
-    if (n) {
-        FGB_CUDA(cudaMemcpyAsync(b->x[c].p + f, b->st_x.p, n * sizeof(float4), cudaMemcpyHostToDevice, st), "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->v[c].p + f, b->st_v.p, n * sizeof(float4), cudaMemcpyHostToDevice, st), "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->type[c].p + f, b->st_type.p, n * sizeof(int32_t), cudaMemcpyHostToDevice, st),
-                 "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->col[c].p + f, b->st_col.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
-                 "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->slot[c].p + f, b->st_slot.p, n * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
-                 "upload");
-    }
     // the scene's key prefix, in case a surface call precedes the first step
     launch_fill_u32(b->keys_sorted.p + f, n, b->mbits >= 32 ? 0u : (k << b->mbits), st);
-    FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
+    // the staging buffers are only rewritten after a synchronisation (the next
+    // upload's, or a download's), so the copies may still be running on return
     return FGB_OK;
 }
 
@@ -939,38 +1032,57 @@ static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
     FGB_CUDA(b->st_slot.ensure(n), "download staging");
     cudaStream_t st = b->stream();
     const int c = b->cur;
-    if (n) {
-        FGB_CUDA(cudaMemcpyAsync(b->st_x.p, b->x[c].p + f, n * sizeof(float4), cudaMemcpyDeviceToHost, st), "download");
-        FGB_CUDA(cudaMemcpyAsync(b->st_v.p, b->v[c].p + f, n * sizeof(float4), cudaMemcpyDeviceToHost, st), "download");
-        FGB_CUDA(cudaMemcpyAsync(b->st_type.p, b->type[c].p + f, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
+    // every piece's copies are queued first, each followed by an event; the host
+    // threads unpack a piece as soon as its event has passed
+    const uint64_t piece = std::max<uint64_t>(kPieceMin, (n + kPieces - 1) / kPieces);
+    uint32_t pieces = 0;
+    for (uint64_t p0 = 0; p0 < n; p0 += piece, ++pieces) {
+        const uint64_t m = std::min(n - p0, piece), d = f + p0;
+        if (b->piece_events.size() <= pieces) {
+            cudaEvent_t e;
+            FGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "download events");
+            b->piece_events.push_back(e);
+        }
+        FGB_CUDA(cudaMemcpyAsync(b->st_x.p + p0, b->x[c].p + d, m * sizeof(float4), cudaMemcpyDeviceToHost, st),
                  "download");
-        FGB_CUDA(cudaMemcpyAsync(b->st_col.p, b->col[c].p + f, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+        FGB_CUDA(cudaMemcpyAsync(b->st_v.p + p0, b->v[c].p + d, m * sizeof(float4), cudaMemcpyDeviceToHost, st),
                  "download");
-        FGB_CUDA(cudaMemcpyAsync(b->st_slot.p, b->slot[c].p + f, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+        FGB_CUDA(cudaMemcpyAsync(b->st_type.p + p0, b->type[c].p + d, m * sizeof(int32_t), cudaMemcpyDeviceToHost, st),
                  "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_col.p + p0, b->col[c].p + d, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                 "download");
+        FGB_CUDA(cudaMemcpyAsync(b->st_slot.p + p0, b->slot[c].p + d, m * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                 st),
+                 "download");
+        FGB_CUDA(cudaEventRecord(b->piece_events[pieces], st), "download event");
+    }
+    const std::vector<uint64_t> &ids = b->ids[k];
+    uint32_t q = 0;
+    for (uint64_t p0 = 0; p0 < n; p0 += piece, ++q) {
+        const uint64_t m = std::min(n - p0, piece);
+        FGB_CUDA(cudaEventSynchronize(b->piece_events[q]), "download sync");
+        parallel_for(m, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = p0 + lo; i < p0 + hi; ++i) {
+                const float4 X = b->st_x.p[i], V = b->st_v.p[i];
+                if (xs->position) {
+                    xs->position[3 * i] = X.x;
+                    xs->position[3 * i + 1] = X.y;
+                    xs->position[3 * i + 2] = X.z;
+                }
+                if (xs->mass) xs->mass[i] = X.w;
+                if (xs->velocity) {
+                    xs->velocity[3 * i] = V.x;
+                    xs->velocity[3 * i + 1] = V.y;
+                    xs->velocity[3 * i + 2] = V.z;
+                }
+                if (xs->type) xs->type[i] = b->st_type.p[i];
+                if (xs->colour) xs->colour[i] = b->st_col.p[i];
+                const uint32_t sl = b->st_slot.p[i];
+                if (xs->id) xs->id[i] = sl < ids.size() ? ids[sl] : sl;
+            }
+        });
     }
     FGB_CUDA(cudaStreamSynchronize(st), "download sync");
-    const std::vector<uint64_t> &ids = b->ids[k];
-    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
-        for (uint64_t i = lo; i < hi; ++i) {
-            const float4 X = b->st_x.p[i], V = b->st_v.p[i];
-            if (xs->position) {
-                xs->position[3 * i] = X.x;
-                xs->position[3 * i + 1] = X.y;
-                xs->position[3 * i + 2] = X.z;
-            }
-            if (xs->mass) xs->mass[i] = X.w;
-            if (xs->velocity) {
-                xs->velocity[3 * i] = V.x;
-                xs->velocity[3 * i + 1] = V.y;
-                xs->velocity[3 * i + 2] = V.z;
-            }
-            if (xs->type) xs->type[i] = b->st_type.p[i];
-            if (xs->colour) xs->colour[i] = b->st_col.p[i];
-            const uint32_t sl = b->st_slot.p[i];
-            if (xs->id) xs->id[i] = sl < ids.size() ? ids[sl] : sl;
-        }
-    });
     return FGB_OK;
 }
 
