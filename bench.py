@@ -214,12 +214,32 @@ def bench_batched(params, steps=20, mc_every=10, tune=True):
     for b in singles:
         b.close()
     solver.close()
+    # the plain single-scene step as a libfluid user calls it: one drop-in solver per
+    # scene, advance() per frame with host arrays, a surface every mc_every frames
+    plain = [(SphSolver(params=params), scenes.copy_particles(p), c) for p, c in specs]
+    for sv, p, c in plain:
+        for _ in range(3):
+            sv.advance(c, p)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(1, steps + 1):
+        for sv, p, c in plain:
+            c.surface = 1 if s % mc_every == 0 else 0
+            sv.advance(c, p)
+            c.surface = 0
+    t_plain = time.perf_counter() - t0
+    for sv, _, _ in plain:
+        sv.close()
     torch.cuda.synchronize()
     v_b = total * steps / t_batched
     v_l = total * steps / t_loop
+    v_p = total * steps / t_plain
     return {"workload": "batched_64", "scenes": len(specs), "particles": total, "steps": steps,
             "surface_every": mc_every, "batched_particle_steps_per_s": v_b, "per_scene_loop_particle_steps_per_s": v_l,
-            "speedup": v_b / v_l, "batched_launches": launches, "triangles": tris}
+            "speedup": v_b / v_l, "per_scene_advance_loop_particle_steps_per_s": v_p,
+            "speedup_vs_advance_loop": v_b / v_p, "batched_launches": launches, "triangles": tris,
+            "arms": "batched: one resident batch; loop: the same scenes as resident single-scene batches; "
+                    "advance loop: one drop-in solver per scene, advance() with host arrays every frame"}
 
 
 def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=0):

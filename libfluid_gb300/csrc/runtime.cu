@@ -1499,8 +1499,11 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     if (n_colliders && !colliders) return fail(FGB_ERR_INVALID, "advance: null colliders");
     if (mesh_out) mesh_out->n = 0;
     if (xs->n == 0) return FGB_OK;  // oclsph.hpp:711-715 returns an empty result
-    const bool same = s->cached && s->cached_n == xs->n &&
-                      memcmp(&s->cached_cfg, cfg, sizeof(fgb_config)) == 0;
+    // `surface` only says whether this frame also extracts a surface: it does not
+    // change the resident scene, so frames that differ in it reuse the same batch
+    fgb_config key = *cfg;
+    key.surface = s->cached_cfg.surface;
+    const bool same = s->cached && s->cached_n == xs->n && memcmp(&s->cached_cfg, &key, sizeof(fgb_config)) == 0;
     if (!same) {
         if (s->cached) destroy_batch(s->cached);
         s->cached = nullptr;

@@ -368,3 +368,22 @@ def test_autotune_changes_no_result():
         x.close()
     tuned_solver.close()
     plain_solver.close()
+
+
+def test_advance_surface_frames_do_not_change_the_state():
+    # asking for a surface on some frames changes nothing in the particles: the
+    # drop-in keeps its resident scene across frames that differ only in that flag
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = scenes.dam_break((16, 16, 16), (1.6, 1.6, 1.6), seed=71)
+    a, b = scenes.copy_particles(parts), scenes.copy_particles(parts)
+    sa, sb = SphSolver(params=params), SphSolver(params=params)
+    for frame in range(6):
+        cfg.surface = frame % 2
+        mesh = sa.advance(cfg, a)
+        assert (mesh is not None and len(mesh) > 0) == bool(frame % 2)
+        cfg.surface = 0
+        sb.advance(cfg, b)
+    for f in ("id", "position", "velocity", "colour"):
+        assert (a[f] == b[f]).all(), f
+    sa.close()
+    sb.close()
