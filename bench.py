@@ -498,8 +498,9 @@ def run_ours(args):
 
 
 def ncu_case():
-    """Four plain steps of dam_break_1m: per step, predict, 2 + passes sort kernels,
-    reorder, 4 x (lambda, delta), 2 vorticity kernels."""
+    """Four plain steps of dam_break_1m (per step: predict, 2 + passes sort kernels,
+    reorder, 4 x (lambda, delta), 2 vorticity kernels), then one surface of the
+    256x128x128-cube lattice (position keys, sort, gather, field, scan, emit)."""
     from libfluid_gb300 import build, capi, scenes
     from libfluid_gb300.solver import Batch, SphSolver
     build.build()
@@ -509,7 +510,8 @@ def ncu_case():
     batch = Batch(solver, [(parts, cfg)])
     batch.step(4)
     batch.sync()
-    print("ncu case done, error flags", batch.error_flags())
+    tris = batch.surface(0)
+    print("ncu case done, error flags", batch.error_flags(), "triangles", len(tris))
     batch.close()
     solver.close()
 
