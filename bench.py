@@ -436,14 +436,16 @@ def run_ours(args):
     step_total = sum(stage_sum) / args.steps
 
     # end to end through the reference-facing call with host buffers
-    e2e_steps = max(3, min(args.steps, 10))
+    # the same window of the dam break as the device-resident measurement: W frames
+    # of warm-up, then K timed frames
+    e2e_steps = args.steps
     host = scenes.copy_particles(parts)
     e2e_solver = SphSolver(params=params)
     if tuned is not None:
         t = Batch(e2e_solver, [(scenes.copy_particles(parts), cfg)])
         t.autotune(3)
         t.close()
-    for _ in range(2):
+    for _ in range(args.warmup):
         e2e_solver.advance(cfg, host)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
