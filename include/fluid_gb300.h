@@ -125,7 +125,8 @@ int fgb_version(void);
 const char *fgb_last_error(void);
 /* sizeof of the ABI structs in this order: fgb_params, fgb_config, fgb_particles,
  * fgb_triangle, fgb_mesh_triangle, fgb_mesh, fgb_grid_info, fgb_well,
- * fgb_serve_options, fgb_serve_result, fgb_serve_stats, fgb_tune_result; writes at most
+ * fgb_serve_options, fgb_serve_result, fgb_serve_stats, fgb_tune_result, fgb_source,
+ * fgb_drain; writes at most
  * n values and returns how many exist.  Replaces the reference's check_size kernel
  * and host assert of struct layouts (oclsph_kernel.h:276-278, oclsph.hpp:217-243). */
 int fgb_struct_sizes(uint64_t *out, int n);
@@ -226,6 +227,29 @@ int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out);
  * particle count, same solver).  The particle order is kept, so the scene's later
  * steps are bit-identical to what src would have computed. */
 int fgb_batch_copy_scene(fgb_batch *dst, uint32_t dst_scene, fgb_batch *src, uint32_t src_scene);
+
+/* Sources and drains of a resident scene, applied where the particles are: the
+ * reference's per-frame CPU pass over the particle vector (oclsph.hpp:675-708).
+ * Each source appends floor(sqrt(rate)) x ceil(sqrt(rate)) fluid particles of mass
+ * 1 on a lattice of spacing h*scale/2 in the xz plane centred on `centre`, with the
+ * source's velocity, colour and tag as id; then every fluid particle (the new ones
+ * included) closer than `width` to a drain's centre is removed.  Survivors keep
+ * their order, the new particles follow the scene's survivors, and later scenes
+ * follow as before.  Only the emitted particles cross the bus; the arrays grow on
+ * the device when the batch needs more room.  *count receives the scene's new
+ * particle count.  (fluid.hpp:147-169: Source, Drain.) */
+typedef struct fgb_source {
+    float centre[3];
+    float velocity[3];
+    uint64_t rate, tag;
+    uint32_t colour;
+} fgb_source;
+typedef struct fgb_drain {
+    float centre[3];
+    float width, depth;  /* a particle is drained when closer than width; depth is unused, as in the reference */
+} fgb_drain;
+int fgb_batch_sources_drains(fgb_batch *b, uint32_t scene, const fgb_source *sources, uint32_t n_sources,
+                             const fgb_drain *drains, uint32_t n_drains, uint64_t *count);
 /* Device bytes one scene of n particles occupies in a batch (with its surface
  * buffers when want_mesh); used for admission against an HBM budget. */
 int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, int want_mesh, uint64_t *bytes);

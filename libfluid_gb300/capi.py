@@ -167,6 +167,15 @@ class ServeStats(ctypes.Structure):
     ]
 
 
+class Source(ctypes.Structure):
+    _fields_ = [("centre", f3), ("velocity", f3), ("rate", ctypes.c_uint64), ("tag", ctypes.c_uint64),
+                ("colour", ctypes.c_uint32)]
+
+
+class Drain(ctypes.Structure):
+    _fields_ = [("centre", f3), ("width", ctypes.c_float), ("depth", ctypes.c_float)]
+
+
 class TuneResult(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("skin", ctypes.c_float), ("ms_per_step", ctypes.c_float),
                 ("trials", ctypes.c_uint32), ("steps", ctypes.c_uint32)]
@@ -200,6 +209,8 @@ _SIGS = {
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),
     "fgb_batch_set_timing": (ctypes.c_int, [c_void_p, ctypes.c_int]),
     "fgb_batch_autotune": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(TuneResult)]),
+    "fgb_batch_sources_drains": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(Source), ctypes.c_uint32, P(Drain),
+                                                ctypes.c_uint32, P(ctypes.c_uint64)]),
     "fgb_batch_stage_times": (ctypes.c_int, [c_void_p, P(ctypes.c_float), ctypes.c_uint32, P(ctypes.c_uint32)]),
     "fgb_batch_probe_size": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(ctypes.c_uint64)]),
     "fgb_batch_probe": (ctypes.c_int, [c_void_p, ctypes.c_uint32, c_void_p, ctypes.c_uint64]),

@@ -110,6 +110,19 @@ struct ResidentScene {
 int batch_resident(fgb_batch *b, uint32_t scene, ResidentScene *out);
 void *batch_wire_scratch(fgb_batch *b, uint64_t bytes);  // device staging, grown on demand
 
+// sources and drains of a resident scene (edit.cu)
+struct SceneMove {
+    uint64_t first_old, first_new;  // a scene's first particle before and after the edit
+};
+void launch_drain_flags(uint64_t n, uint32_t mbits, uint32_t scene, const uint32_t *keys, const float4 *x,
+                        const int32_t *type, const fgb_drain *drains, uint32_t n_drains, uint32_t *keep,
+                        cudaStream_t st);
+void launch_edit_scatter(uint64_t n, uint32_t mbits, uint32_t scene, uint64_t emitted, const uint32_t *keys,
+                         const uint32_t *keep, const uint32_t *rank, const SceneMove *moves, const float4 *x0,
+                         const float4 *v0, const int32_t *t0, const uint32_t *c0, const uint32_t *s0,
+                         const uint64_t *ids0, float4 *x1, float4 *v1, int32_t *t1, uint32_t *c1, uint32_t *s1,
+                         uint64_t *ids1, cudaStream_t st);
+
 // vertex welding of device-resident triangles (weld.cu)
 int weld_device(const fgb_mesh_triangle *d_tris, uint64_t n_tris, uint32_t *d_index, float *d_vertices,
                 uint64_t *n_vertices, cudaStream_t st);

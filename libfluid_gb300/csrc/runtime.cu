@@ -79,6 +79,10 @@ struct Dev {
         else p = nullptr;
         return e;
     }
+    void swap(Dev &o) {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+    }
 };
 
 template <class T>
@@ -323,6 +327,7 @@ struct fgb_batch {
     std::vector<fgb_config> cfg;
     std::vector<uint64_t> counts, first;
     uint64_t n = 0;
+    uint64_t capacity = 0;  // particles the per-particle arrays hold (>= n)
     uint32_t mbits = 0, sbits = 0, key_bits = 0, iterations = 0;
     std::vector<SceneDev> h_scenes;
     Dev<SceneDev> d_scenes;
@@ -755,6 +760,44 @@ static int mesh_assign(fgb_mesh *m, const fgb_mesh_triangle *dev, uint64_t count
     return FGB_OK;
 }
 
+// The per-particle arrays a step rebuilds (sort keys, p*, lists, lambda, ...), for
+// `cap` particles; their contents do not outlive a step.
+static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
+    const fgb_params &p = b->solver->params;
+    for (int c = 0; c < 2; ++c) FGB_CUDA(b->ps[c].alloc(cap), "batch alloc");
+    FGB_CUDA(b->keys_in.alloc(cap), "batch alloc");
+    FGB_CUDA(b->vals_in.alloc(cap), "batch alloc");
+    FGB_CUDA(b->keys_sorted.alloc(cap), "batch alloc");
+    FGB_CUDA(b->vals_sorted.alloc(cap), "batch alloc");
+    b->sort_scratch_bytes = radix_scratch_bytes(cap);
+    FGB_CUDA(b->sort_scratch.alloc(b->sort_scratch_bytes), "batch alloc");
+    FGB_CUDA(b->ps_grid.alloc(cap), "batch alloc");
+    if (b->list_cap) {
+        FGB_CUDA(b->nlist.alloc(cap * b->list_cap), "batch alloc neighbour lists");
+        FGB_CUDA(b->ncount.alloc(cap), "batch alloc");
+        FGB_CUDA(b->disp.alloc(cap), "batch alloc");
+        FGB_CUDA(b->valid.alloc(cap), "batch alloc");
+    }
+    if (b->hit_cap) {
+        FGB_CUDA(b->hlist.alloc(cap * b->hit_cap), "batch alloc hit lists");
+        FGB_CUDA(b->hcount.alloc(cap), "batch alloc");
+    }
+    FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
+    FGB_CUDA(b->density.alloc(cap), "batch alloc");
+    if (p.profile != FGB_PROFILE_REF) {
+        FGB_CUDA(b->omega.alloc(cap), "batch alloc");
+        FGB_CUDA(b->vx.alloc(cap), "batch alloc");
+    } else {
+        FGB_CUDA(b->colour_sums.alloc(cap), "batch alloc");
+        FGB_CUDA(b->colour_count.alloc(cap), "batch alloc");
+    }
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemsetAsync(b->lambda.p, 0, cap * sizeof(float), st), "batch alloc");
+    FGB_CUDA(cudaMemsetAsync(b->density.p, 0, cap * sizeof(float), st), "batch alloc");
+    b->capacity = cap;
+    return FGB_OK;
+}
+
 static int batch_init(fgb_batch *b) {
     fgb_solver *s = b->solver;
     const fgb_params &p = s->params;
@@ -818,17 +861,9 @@ static int batch_init(fgb_batch *b) {
         FGB_CUDA(b->type[c].alloc(n), "batch alloc");
         FGB_CUDA(b->col[c].alloc(n), "batch alloc");
         FGB_CUDA(b->slot[c].alloc(n), "batch alloc");
-        if (c == 0) FGB_CUDA(b->ids_dev.alloc(n), "batch alloc");
-        FGB_CUDA(b->ps[c].alloc(n), "batch alloc");
     }
-    FGB_CUDA(b->keys_in.alloc(n), "batch alloc");
-    FGB_CUDA(b->vals_in.alloc(n), "batch alloc");
-    FGB_CUDA(b->keys_sorted.alloc(n), "batch alloc");
-    FGB_CUDA(b->vals_sorted.alloc(n), "batch alloc");
-    b->sort_scratch_bytes = radix_scratch_bytes(n);
-    FGB_CUDA(b->sort_scratch.alloc(b->sort_scratch_bytes), "batch alloc");
+    FGB_CUDA(b->ids_dev.alloc(n), "batch alloc");
     FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
-    FGB_CUDA(b->ps_grid.alloc(n), "batch alloc");
     if (const char *e = getenv("FGB_LIST_CAP")) b->list_cap = (uint32_t)atoi(e);
     b->block = s->block;
     {
@@ -841,37 +876,18 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
-    if (b->list_cap) {
-        FGB_CUDA(b->nlist.alloc(n * b->list_cap), "batch alloc neighbour lists");
-        FGB_CUDA(b->ncount.alloc(n), "batch alloc");
-        FGB_CUDA(b->disp.alloc(n), "batch alloc");
-        FGB_CUDA(b->valid.alloc(n), "batch alloc");
-        FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
-    }
+    if (b->list_cap) FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
     if (const char *e = getenv("FGB_HIT_CAP")) b->hit_cap = (uint32_t)atoi(e);
     if (b->hit_cap > 4096) b->hit_cap = 4096;
     b->hit_cap = (b->hit_cap + 3u) & ~3u;  // rows move as 16-byte vectors
-    if (b->hit_cap) {
-        FGB_CUDA(b->hlist.alloc(n * b->hit_cap), "batch alloc hit lists");
-        FGB_CUDA(b->hcount.alloc(n), "batch alloc");
-    }
-    FGB_CUDA(b->lambda.alloc(n), "batch alloc");
-    FGB_CUDA(b->density.alloc(n), "batch alloc");
-    if (p.profile != FGB_PROFILE_REF) {
-        FGB_CUDA(b->omega.alloc(n), "batch alloc");
-        FGB_CUDA(b->vx.alloc(n), "batch alloc");
-    } else {
-        FGB_CUDA(b->colour_sums.alloc(n), "batch alloc");
-        FGB_CUDA(b->colour_count.alloc(n), "batch alloc");
-    }
+    int rc = alloc_step_arrays(b, n);
+    if (rc) return rc;
     FGB_CUDA(b->err.alloc(1), "batch alloc");
     FGB_CUDA(b->d_scenes.alloc(b->n_scenes), "batch alloc");
     FGB_CUDA(b->d_wells.alloc(std::max<size_t>(wells.size(), 1)), "batch alloc");
     FGB_CUDA(b->d_tris.alloc(1), "batch alloc");
     cudaStream_t st = b->stream();
     FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), st), "batch init");
-    FGB_CUDA(cudaMemsetAsync(b->lambda.p, 0, n * sizeof(float), st), "batch init");
-    FGB_CUDA(cudaMemsetAsync(b->density.p, 0, n * sizeof(float), st), "batch init");
     if (!wells.empty())
         FGB_CUDA(cudaMemcpyAsync(b->d_wells.p, wells.data(), wells.size() * sizeof(WellDev), cudaMemcpyHostToDevice, st),
                  "batch init");
@@ -1128,7 +1144,8 @@ int fgb_struct_sizes(uint64_t *out, int n) {
     const uint64_t sizes[] = {sizeof(fgb_params), sizeof(fgb_config),        sizeof(fgb_particles),
                               sizeof(fgb_triangle), sizeof(fgb_mesh_triangle), sizeof(fgb_mesh),
                               sizeof(fgb_grid_info), sizeof(fgb_well),          sizeof(fgb_serve_options),
-                              sizeof(fgb_serve_result), sizeof(fgb_serve_stats), sizeof(fgb_tune_result)};
+                              sizeof(fgb_serve_result), sizeof(fgb_serve_stats), sizeof(fgb_tune_result),
+                              sizeof(fgb_source),       sizeof(fgb_drain)};
     const int m = (int)(sizeof(sizes) / sizeof(sizes[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = sizes[i];
     return m;
@@ -1465,6 +1482,161 @@ int fgb_batch_copy_scene(fgb_batch *dst, uint32_t dst_scene, fgb_batch *src, uin
     if (!dst || !src) return fail(FGB_ERR_INVALID, "copy_scene: null batch");
     if (dst->solver != src->solver) return fail(FGB_ERR_INVALID, "copy_scene: batches of different solvers");
     return batch_copy_scene(dst, dst_scene, src, src_scene);
+}
+
+int fgb_batch_sources_drains(fgb_batch *b, uint32_t k, const fgb_source *sources, uint32_t n_sources,
+                             const fgb_drain *drains, uint32_t n_drains, uint64_t *count) {
+    if (!b || !count || k >= b->n_scenes) return fail(FGB_ERR_INVALID, "sources_drains: bad argument");
+    if ((n_sources && !sources) || (n_drains && !drains)) return fail(FGB_ERR_INVALID, "sources_drains: null array");
+    const fgb_config &c = b->cfg[k];
+    // emission (oclsph.hpp:678-691), with the drain test of 694-705 applied to the
+    // new particles right away, as the reference erases after emitting
+    const float spacing = (b->solver->params.h * c.scale / 2);
+    auto drained = [&](const float *pos) {
+        for (uint32_t d = 0; d < n_drains; ++d) {
+            const float dx = drains[d].centre[0] - pos[0], dy = drains[d].centre[1] - pos[1],
+                        dz = drains[d].centre[2] - pos[2];
+            if (std::sqrt(dx * dx + dy * dy + dz * dz) < drains[d].width) return true;
+        }
+        return false;
+    };
+    std::vector<float4> ex, ev;
+    std::vector<uint64_t> eid;
+    std::vector<uint32_t> ecol;
+    for (uint32_t q = 0; q < n_sources; ++q) {
+        const fgb_source &src = sources[q];
+        const float size = (float)std::sqrt((double)src.rate);
+        const int width = (int)std::floor(size), depth = (int)std::ceil(size);
+        const float off[3] = {src.centre[0] - ((float)width / 2.f) * spacing, src.centre[1] - (0.f / 2.f) * spacing,
+                              src.centre[2] - ((float)depth / 2.f) * spacing};
+        for (int x = 0; x < width; ++x)
+            for (int z = 0; z < depth; ++z) {
+                const float pos[3] = {off[0] + (float)x * spacing, off[1] + 0.f * spacing, off[2] + (float)z * spacing};
+                if (drained(pos)) continue;
+                ex.push_back(make_float4(pos[0], pos[1], pos[2], 1.f));
+                ev.push_back(make_float4(src.velocity[0], src.velocity[1], src.velocity[2], 0.f));
+                eid.push_back(src.tag);
+                ecol.push_back(src.colour);
+            }
+    }
+    const uint64_t E = ex.size(), n0 = b->n;
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaStreamSynchronize(st), "sources_drains sync");
+    // survivors: drain flags, their exclusive scan
+    Dev<uint32_t> keep, rank, total;
+    Dev<char> scratch;
+    Dev<fgb_drain> d_drains;
+    Dev<SceneMove> d_moves;
+    const uint64_t sb = scan_u32_scratch_bytes(n0);
+    FGB_CUDA(keep.alloc(n0), "sources_drains alloc");
+    FGB_CUDA(rank.alloc(n0), "sources_drains alloc");
+    FGB_CUDA(total.alloc(1), "sources_drains alloc");
+    FGB_CUDA(scratch.alloc(sb), "sources_drains alloc");
+    FGB_CUDA(d_drains.alloc(std::max<uint32_t>(n_drains, 1)), "sources_drains alloc");
+    FGB_CUDA(d_moves.alloc(b->n_scenes), "sources_drains alloc");
+    if (n_drains)
+        FGB_CUDA(cudaMemcpyAsync(d_drains.p, drains, n_drains * sizeof(fgb_drain), cudaMemcpyHostToDevice, st),
+                 "sources_drains drains");
+    const int cs = b->cur, cn = cs ^ 1;
+    launch_drain_flags(n0, b->mbits, k, b->keys_sorted.p, b->x[cs].p, b->type[cs].p, d_drains.p, n_drains, keep.p, st);
+    uint32_t kept_all = 0;
+    if (n0) {
+        cudaError_t e = scan_u32(keep.p, rank.p, total.p, n0, scratch.p, sb, st, b->err.p, nullptr);
+        if (e != cudaSuccess) return fail_cuda(e, "sources_drains scan");
+        FGB_CUDA(cudaMemcpyAsync(&kept_all, total.p, sizeof kept_all, cudaMemcpyDeviceToHost, st), "sources_drains");
+        FGB_CUDA(cudaStreamSynchronize(st), "sources_drains sync");
+    }
+    const uint64_t kept_k = kept_all - (n0 - b->counts[k]);
+    // the new layout
+    std::vector<uint64_t> counts = b->counts, first(b->n_scenes);
+    counts[k] = kept_k + E;
+    std::vector<SceneMove> moves(b->n_scenes);
+    uint64_t n1 = 0;
+    for (uint32_t s = 0; s < b->n_scenes; ++s) {
+        first[s] = n1;
+        moves[s] = SceneMove{b->first[s], n1};
+        n1 += counts[s];
+    }
+    if (n1 > 0x7fffffffull) return fail(FGB_ERR_CAPACITY, "sources_drains: more than 2^31-1 particles");
+    const bool grow = n1 > b->capacity;
+    const uint64_t cap = grow ? std::max<uint64_t>(n1, b->capacity + b->capacity / 4) : b->capacity;
+    if (grow) {
+        FGB_CUDA(b->x[cn].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->v[cn].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->type[cn].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->col[cn].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->slot[cn].alloc(cap), "sources_drains grow");
+    }
+    Dev<uint64_t> ids1;
+    FGB_CUDA(ids1.alloc(cap), "sources_drains alloc");
+    FGB_CUDA(cudaMemcpyAsync(d_moves.p, moves.data(), b->n_scenes * sizeof(SceneMove), cudaMemcpyHostToDevice, st),
+             "sources_drains moves");
+    launch_edit_scatter(n0, b->mbits, k, E, b->keys_sorted.p, keep.p, rank.p, d_moves.p, b->x[cs].p, b->v[cs].p,
+                        b->type[cs].p, b->col[cs].p, b->slot[cs].p, b->ids_dev.p, b->x[cn].p, b->v[cn].p,
+                        b->type[cn].p, b->col[cn].p, b->slot[cn].p, ids1.p, st);
+    FGB_CUDA(cudaGetLastError(), "sources_drains scatter");
+    if (E) {  // the emitted particles, after the scene's survivors
+        FGB_CUDA(b->st_x.ensure(E), "sources_drains staging");
+        FGB_CUDA(b->st_v.ensure(E), "sources_drains staging");
+        FGB_CUDA(b->st_type.ensure(E), "sources_drains staging");
+        FGB_CUDA(b->st_col.ensure(E), "sources_drains staging");
+        FGB_CUDA(b->st_slot.ensure(E), "sources_drains staging");
+        FGB_CUDA(b->st_ids.ensure(E), "sources_drains staging");
+        for (uint64_t e = 0; e < E; ++e) {
+            b->st_x.p[e] = ex[e];
+            b->st_v.p[e] = ev[e];
+            b->st_type.p[e] = FGB_TYPE_FLUID;
+            b->st_col.p[e] = ecol[e];
+            b->st_slot.p[e] = (uint32_t)(kept_k + e);
+            b->st_ids.p[e] = eid[e];
+        }
+        const uint64_t d = first[k] + kept_k;
+        FGB_CUDA(cudaMemcpyAsync(b->x[cn].p + d, b->st_x.p, E * sizeof(float4), cudaMemcpyHostToDevice, st), "emit");
+        FGB_CUDA(cudaMemcpyAsync(b->v[cn].p + d, b->st_v.p, E * sizeof(float4), cudaMemcpyHostToDevice, st), "emit");
+        FGB_CUDA(cudaMemcpyAsync(b->type[cn].p + d, b->st_type.p, E * sizeof(int32_t), cudaMemcpyHostToDevice, st),
+                 "emit");
+        FGB_CUDA(cudaMemcpyAsync(b->col[cn].p + d, b->st_col.p, E * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "emit");
+        FGB_CUDA(cudaMemcpyAsync(b->slot[cn].p + d, b->st_slot.p, E * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
+                 "emit");
+        FGB_CUDA(cudaMemcpyAsync(ids1.p + d, b->st_ids.p, E * sizeof(uint64_t), cudaMemcpyHostToDevice, st), "emit");
+    }
+    FGB_CUDA(cudaStreamSynchronize(st), "sources_drains sync");
+    if (grow) {  // the old set and the per-step arrays, at the new capacity
+        FGB_CUDA(b->x[cs].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->v[cs].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->type[cs].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->col[cs].alloc(cap), "sources_drains grow");
+        FGB_CUDA(b->slot[cs].alloc(cap), "sources_drains grow");
+        int rc = alloc_step_arrays(b, cap);
+        if (rc) return rc;
+    }
+    b->ids_dev.swap(ids1);
+    b->cur = cn;
+    b->counts = counts;
+    b->first = first;
+    b->n = n1;
+    for (uint32_t s = 0; s < b->n_scenes; ++s) {
+        b->h_scenes[s].first = (uint32_t)first[s];
+        b->h_scenes[s].count = (uint32_t)counts[s];
+        // every scene's key prefix for the next step's scene lookup
+        launch_fill_u32(b->keys_sorted.p + first[s], counts[s], b->mbits >= 32 ? 0u : (s << b->mbits), st);
+    }
+    b->tris_dirty = true;   // re-uploads the scene table
+    b->surf_ready = false;  // surface buffers are sized by the particle count
+    b->surf_tri_first.clear();
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    b->graphs_ok = false;
+    // the scene's ids by its new slots, for downloads
+    b->ids[k].assign(counts[k], 0);
+    if (counts[k])
+        FGB_CUDA(cudaMemcpyAsync(b->ids[k].data(), b->ids_dev.p + first[k], counts[k] * sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, st),
+                 "sources_drains ids");
+    FGB_CUDA(cudaStreamSynchronize(st), "sources_drains sync");
+    *count = counts[k];
+    return FGB_OK;
 }
 
 int fgb_scene_footprint(const fgb_solver *s, const fgb_config *cfg, uint64_t n, int want_mesh, uint64_t *bytes) {

@@ -122,6 +122,24 @@ class Batch:
     def sync(self):
         capi.check(self.lib.fgb_batch_sync(self._h))
 
+    def sources_drains(self, k, sources=(), drains=()):
+        """Apply sources [(centre, velocity, rate, tag, colour)] and drains
+        [(centre, width)] to resident scene k on the device; returns its new count."""
+        srcs = (capi.Source * max(len(sources), 1))()
+        for i, (centre, vel, rate, tag, colour) in enumerate(sources):
+            srcs[i].centre[:] = centre
+            srcs[i].velocity[:] = vel
+            srcs[i].rate, srcs[i].tag, srcs[i].colour = rate, tag, colour
+        drs = (capi.Drain * max(len(drains), 1))()
+        for i, (centre, width) in enumerate(drains):
+            drs[i].centre[:] = centre
+            drs[i].width = width
+        count = ctypes.c_uint64()
+        capi.check(self.lib.fgb_batch_sources_drains(self._h, k, srcs, len(sources), drs, len(drains),
+                                                     ctypes.byref(count)))
+        self.counts[k] = int(count.value)
+        return self.counts[k]
+
     def autotune(self, steps_per_trial=3):
         """Pick the fastest launch shape on this batch's next steps (they are ordinary
         steps) and cache it in the solver for its size bucket; returns TuneResult."""
