@@ -477,7 +477,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}", "cuda_graph": True,
                        "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
                                       "trial_steps": int(tuned.steps)} if tuned else None)},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 48 * n, "d2h_bytes_per_step": 44 * n,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 40 * n, "d2h_bytes_per_step": 44 * n,
                     "steps": e2e_steps, "call": "fgb_advance"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,

@@ -77,6 +77,7 @@ struct StepView {
 constexpr uint16_t kListOverflow = 0xffffu;
 
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t value, cudaStream_t st);
+void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);

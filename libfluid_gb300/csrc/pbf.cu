@@ -885,6 +885,19 @@ __global__ void k_fill_u32(uint32_t *__restrict__ p, uint64_t n, uint32_t value)
 }
 }  // namespace
 
+namespace {
+__global__ void k_iota_u32(uint32_t *__restrict__ p, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = (uint32_t)i;
+}
+}  // namespace
+
+void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st) {
+    if (!n) return;
+    unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256, 152u * 8u);
+    k_iota_u32<<<g, 256, 0, st>>>(p, n);
+}
+
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t value, cudaStream_t st) {
     if (!n) return;
     unsigned g = (unsigned)std::min<uint64_t>((n + 255) / 256, 152u * 8u);

@@ -341,6 +341,7 @@ struct fgb_batch {
     Dev<int32_t> type[2];
     Dev<uint32_t> col[2], slot[2];
     Dev<uint64_t> ids_dev;  // particle ids by upload slot (scene segment), for device-side record packing
+    std::vector<uint8_t> ids_stale;  // per scene: ids_dev not yet given the last upload's ids (sync_ids)
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -903,7 +904,32 @@ static int batch_init(fgb_batch *b) {
              "batch init");
     FGB_CUDA(cudaStreamSynchronize(st), "batch init");
     b->ids.assign(b->n_scenes, {});
+    b->ids_stale.assign(b->n_scenes, 0);
     b->scene_tris.assign(b->n_scenes, {});
+    return FGB_OK;
+}
+
+// Give ids_dev the ids of every scene uploaded since the last call (the wire
+// packers, scene copies and source/drain edits read it; steps do not).
+static int sync_ids(fgb_batch *b) {
+    cudaStream_t st = b->stream();
+    for (uint32_t k = 0; k < b->n_scenes; ++k) {
+        if (!b->ids_stale[k]) continue;
+        const uint64_t n = b->counts[k];
+        if (n) {
+            FGB_CUDA(cudaStreamSynchronize(st), "ids sync");
+            FGB_CUDA(b->st_ids.ensure(n), "ids staging");
+            const uint64_t *src = b->ids[k].data();
+            parallel_for(n, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t i = lo; i < hi; ++i) b->st_ids.p[i] = src[i];
+            });
+            FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + b->first[k], b->st_ids.p, n * sizeof(uint64_t),
+                                     cudaMemcpyHostToDevice, st),
+                     "ids upload");
+            FGB_CUDA(cudaStreamSynchronize(st), "ids sync");
+        }
+        b->ids_stale[k] = 0;
+    }
     return FGB_OK;
 }
 
@@ -917,10 +943,8 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     FGB_CUDA(b->st_v.ensure(n), "upload staging");
     FGB_CUDA(b->st_type.ensure(n), "upload staging");
     FGB_CUDA(b->st_col.ensure(n), "upload staging");
-    FGB_CUDA(b->st_slot.ensure(n), "upload staging");
     cudaStream_t st = b->stream();
     FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
-    FGB_CUDA(b->st_ids.ensure(n), "upload staging");
     b->ids[k].resize(n);
     std::atomic<uint32_t> obstacle_count{0};
     uint64_t *ids = b->ids[k].data();
@@ -938,8 +962,7 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
                 b->st_v.p[i] = make_float4(xs->velocity[3 * i], xs->velocity[3 * i + 1], xs->velocity[3 * i + 2], 0.f);
                 b->st_type.p[i] = xs->type[i];
                 b->st_col.p[i] = xs->colour ? xs->colour[i] : 0xffffffffu;
-                b->st_slot.p[i] = (uint32_t)i;
-                ids[i] = b->st_ids.p[i] = xs->id ? xs->id[i] : i;
+                ids[i] = xs->id ? xs->id[i] : i;
                 obst += xs->type[i] == FGB_TYPE_OBSTACLE;
             }
             obstacle_count += obst;
@@ -953,13 +976,11 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
                  "upload");
         FGB_CUDA(cudaMemcpyAsync(b->col[c].p + d, b->st_col.p + p0, m * sizeof(uint32_t), cudaMemcpyHostToDevice, st),
                  "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->slot[c].p + d, b->st_slot.p + p0, m * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                 st),
-                 "upload");
-        FGB_CUDA(cudaMemcpyAsync(b->ids_dev.p + d, b->st_ids.p + p0, m * sizeof(uint64_t), cudaMemcpyHostToDevice,
-                                 st),
-                 "upload ids");
     }
+    // slot = place at upload; the ids reach the device only when a device-side
+    // consumer asks for them (sync_ids)
+    launch_iota_u32(b->slot[c].p + f, n, st);
+    b->ids_stale[k] = 1;
     const uint32_t obstacles = obstacle_count.load();
     if (b->h_scenes[k].obstacles != obstacles) {
         b->h_scenes[k].obstacles = obstacles;
@@ -981,7 +1002,10 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
     if (dst->counts[dk] != src->counts[sk]) return fail(FGB_ERR_INVALID, "copy_scene: particle counts differ");
     const uint64_t n = src->counts[sk], fd = dst->first[dk], fs = src->first[sk];
     cudaStream_t st = dst->stream();
+    int rc = sync_ids(src);
+    if (rc) return rc;
     FGB_CUDA(cudaStreamSynchronize(src->stream()), "copy_scene sync");
+    dst->ids_stale[dk] = 0;  // the copy below brings the ids
     const int cd = dst->cur, cs = src->cur;
     if (dst->h_scenes[dk].obstacles != src->h_scenes[sk].obstacles) {
         dst->h_scenes[dk].obstacles = src->h_scenes[sk].obstacles;
@@ -1355,6 +1379,8 @@ extern "C++" {
 namespace fgb {
 int batch_resident(fgb_batch *b, uint32_t k, ResidentScene *out) {
     if (!b || !out || k >= b->n_scenes) return fail(FGB_ERR_INVALID, "resident scene: bad argument");
+    int rc = sync_ids(b);
+    if (rc) return rc;
     const int c = b->cur;
     out->first = b->first[k];
     out->n = b->counts[k];
@@ -1521,6 +1547,8 @@ int fgb_batch_sources_drains(fgb_batch *b, uint32_t k, const fgb_source *sources
     }
     const uint64_t E = ex.size(), n0 = b->n;
     cudaStream_t st = b->stream();
+    int rc0 = sync_ids(b);
+    if (rc0) return rc0;
     FGB_CUDA(cudaStreamSynchronize(st), "sources_drains sync");
     // survivors: drain flags, their exclusive scan
     Dev<uint32_t> keep, rank, total;
