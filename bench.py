@@ -370,6 +370,7 @@ def run_ours(args):
     tuned = tuner.autotune(3) if not args.no_tune else None
     tuner.close()
     batch = Batch(solver, [(parts, cfg)])
+    direct_io = batch.host_io_direct()
     batch.set_timing(True)
     for _ in range(args.warmup):
         batch.step(1)
@@ -477,8 +478,12 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}", "cuda_graph": True,
                        "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
                                       "trial_steps": int(tuned.steps)} if tuned else None)},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 40 * n, "d2h_bytes_per_step": 44 * n,
-                    "steps": e2e_steps, "call": "fgb_advance"},
+            # direct: kernels read id/type/mass/colour/position/velocity (44 B) from the
+            # caller's arrays and write them back; staged: pinned float4 x, float4 v,
+            # type, colour up (40 B), the same plus the upload slot down (44 B)
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": (44 if direct_io else 40) * n,
+                    "d2h_bytes_per_step": 44 * n, "steps": e2e_steps, "call": "fgb_advance",
+                    "host_io": "direct" if direct_io else "staged"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "algorithmic_bytes_per_launch": algo,

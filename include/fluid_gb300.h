@@ -157,6 +157,12 @@ int fgb_batch_create(fgb_solver *s, uint32_t n_scenes, const uint64_t *counts,
                      const fgb_config *configs, fgb_batch **out);
 int fgb_batch_destroy(fgb_batch *b);
 int fgb_batch_upload(fgb_batch *b, uint32_t scene, const fgb_particles *xs);
+/* How uploads and downloads reach the caller's arrays: 1 where kernels read and
+ * write them directly (a device that addresses pageable memory through the host's
+ * page tables, e.g. over Grace's coherent link), 0 where the host packs pinned
+ * staging buffers (elsewhere, or with FGB_HOST_IO=staged at batch creation).
+ * Both give the same bytes; uploads return once the caller's arrays are free. */
+int fgb_batch_host_io(const fgb_batch *b, int *direct);
 int fgb_batch_set_colliders(fgb_batch *b, uint32_t scene, const fgb_triangle *tris, size_t n);
 /* Advance every scene of the batch by `steps` steps: one launch per stage for
  * all scenes, replayed from a CUDA graph. Asynchronous on the solver stream. */

@@ -124,6 +124,26 @@ void launch_edit_scatter(uint64_t n, uint32_t mbits, uint32_t scene, uint64_t em
                          const uint64_t *ids0, float4 *x1, float4 *v1, int32_t *t1, uint32_t *c1, uint32_t *s1,
                          uint64_t *ids1, cudaStream_t st);
 
+// particles between the caller's host arrays and a scene segment, read and written
+// by kernels directly (hostio.cu); only where the device addresses pageable memory
+struct HostParticlesIn {
+    const float *position, *velocity, *mass;  // position/velocity: 3 floats a particle
+    const int32_t *type;
+    const uint32_t *colour;  // may be null: 0xffffffff
+    const uint64_t *id;      // may be null: the index
+};
+struct HostParticlesOut {  // any may be null: not written
+    float *position, *velocity, *mass;
+    int32_t *type;
+    uint32_t *colour;
+    uint64_t *id;
+};
+void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
+                           uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st);
+void launch_unpack_to_host(const HostParticlesOut &out, uint64_t n, const float4 *x, const float4 *v,
+                           const int32_t *type, const uint32_t *col, const uint32_t *slot, const uint64_t *ids,
+                           cudaStream_t st);
+
 // vertex welding of device-resident triangles (weld.cu)
 int weld_device(const fgb_mesh_triangle *d_tris, uint64_t n_tris, uint32_t *d_index, float *d_vertices,
                 uint64_t *n_vertices, cudaStream_t st);

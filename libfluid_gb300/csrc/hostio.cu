@@ -1,0 +1,112 @@
+// hostio.cu -- particles moved between the caller's host arrays and a resident
+// scene by kernels that address the host arrays directly.
+//
+// On a GPU that reads pageable memory through the host's page tables (Grace's
+// coherent link: cudaDevAttrPageableMemoryAccessUsesHostPageTables), a kernel may
+// load from and store to any array the caller allocated.  The packing the
+// reference does on the host before its buffer writes (include/fluid/oclsph.hpp:
+// 822-831, particles into the ClSphAtoms arrays) and the write-back after its
+// read-back (oclsph.hpp:866-892) then run on the GPU: the array-of-structures positions and
+// velocities are read as contiguous runs, regrouped through shared memory into the
+// float4 layout of the device state, and the reverse on the way out, so that every
+// warp access to host memory is a contiguous run of 4-byte words.
+#include <cuda_runtime.h>
+
+#include "fgb_internal.h"
+
+namespace fgb {
+namespace {
+
+constexpr unsigned kTile = 256;  // particles per CTA tile (= threads per CTA)
+
+unsigned grid_of(uint64_t n) {
+    uint64_t g = (n + kTile - 1) / kTile;
+    if (g > 152u * 8u) g = 152u * 8u;
+    return g ? (unsigned)g : 1u;
+}
+
+__global__ void __launch_bounds__(kTile) k_pack_from_host(HostParticlesIn in, uint64_t n, float4 *__restrict__ x,
+                                                         float4 *__restrict__ v, int32_t *__restrict__ type,
+                                                         uint32_t *__restrict__ col, uint32_t *__restrict__ slot,
+                                                         uint64_t *__restrict__ ids, uint32_t *__restrict__ obstacles) {
+    __shared__ float sp[3 * kTile], sv[3 * kTile];
+    const unsigned t = threadIdx.x;
+    uint32_t obst = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTile; base < n; base += (uint64_t)gridDim.x * kTile) {
+        const uint32_t m = (uint32_t)(n - base < kTile ? n - base : kTile);
+        const float *pp = in.position + 3 * base, *pv = in.velocity + 3 * base;
+        for (uint32_t j = t; j < 3 * m; j += kTile) {
+            sp[j] = pp[j];
+            sv[j] = pv[j];
+        }
+        __syncthreads();
+        if (t < m) {
+            const uint64_t i = base + t;
+            const int32_t ty = in.type[i];
+            x[i] = make_float4(sp[3 * t], sp[3 * t + 1], sp[3 * t + 2], in.mass[i]);
+            v[i] = make_float4(sv[3 * t], sv[3 * t + 1], sv[3 * t + 2], 0.f);
+            type[i] = ty;
+            col[i] = in.colour ? in.colour[i] : 0xffffffffu;
+            slot[i] = (uint32_t)i;
+            ids[i] = in.id ? in.id[i] : i;
+            obst += ty == FGB_TYPE_OBSTACLE;
+        }
+        __syncthreads();
+    }
+    // one atomic per warp
+    for (int o = 16; o; o >>= 1) obst += __shfl_xor_sync(0xffffffffu, obst, o);
+    if ((t & 31) == 0 && obst) atomicAdd(obstacles, obst);
+}
+
+__global__ void __launch_bounds__(kTile) k_unpack_to_host(HostParticlesOut out, uint64_t n,
+                                                         const float4 *__restrict__ x, const float4 *__restrict__ v,
+                                                         const int32_t *__restrict__ type,
+                                                         const uint32_t *__restrict__ col,
+                                                         const uint32_t *__restrict__ slot,
+                                                         const uint64_t *__restrict__ ids) {
+    __shared__ float sp[3 * kTile], sv[3 * kTile];
+    const unsigned t = threadIdx.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTile; base < n; base += (uint64_t)gridDim.x * kTile) {
+        const uint32_t m = (uint32_t)(n - base < kTile ? n - base : kTile);
+        if (t < m) {
+            const uint64_t i = base + t;
+            const float4 X = x[i], V = v[i];
+            sp[3 * t] = X.x;
+            sp[3 * t + 1] = X.y;
+            sp[3 * t + 2] = X.z;
+            sv[3 * t] = V.x;
+            sv[3 * t + 1] = V.y;
+            sv[3 * t + 2] = V.z;
+            if (out.mass) out.mass[i] = X.w;
+            if (out.type) out.type[i] = type[i];
+            if (out.colour) out.colour[i] = col[i];
+            if (out.id) {
+                const uint32_t sl = slot[i];
+                out.id[i] = sl < n ? ids[sl] : sl;
+            }
+        }
+        __syncthreads();
+        float *pp = out.position ? out.position + 3 * base : nullptr;
+        float *pv = out.velocity ? out.velocity + 3 * base : nullptr;
+        for (uint32_t j = t; j < 3 * m; j += kTile) {
+            if (pp) pp[j] = sp[j];
+            if (pv) pv[j] = sv[j];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
+                           uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st) {
+    if (n) k_pack_from_host<<<grid_of(n), kTile, 0, st>>>(in, n, x, v, type, col, slot, ids, obstacles);
+}
+
+void launch_unpack_to_host(const HostParticlesOut &out, uint64_t n, const float4 *x, const float4 *v,
+                           const int32_t *type, const uint32_t *col, const uint32_t *slot, const uint64_t *ids,
+                           cudaStream_t st) {
+    if (n) k_unpack_to_host<<<grid_of(n), kTile, 0, st>>>(out, n, x, v, type, col, slot, ids);
+}
+
+}  // namespace fgb

@@ -342,6 +342,8 @@ struct fgb_batch {
     Dev<uint32_t> col[2], slot[2];
     Dev<uint64_t> ids_dev;  // particle ids by upload slot (scene segment), for device-side record packing
     std::vector<uint8_t> ids_stale;  // per scene: ids_dev not yet given the last upload's ids (sync_ids)
+    bool direct = false;    // uploads and downloads address the caller's arrays from kernels (hostio.cu)
+    Dev<uint32_t> obst_dev; // per scene: obstacle count of the last direct upload
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -391,6 +393,7 @@ struct fgb_batch {
     Pinned<int32_t> st_type;
     Pinned<uint32_t> st_col, st_slot, st_keys;
     Pinned<uint64_t> st_ids;
+    Pinned<uint32_t> st_count;
     std::vector<cudaEvent_t> piece_events;  // pipelined download, one per piece
     uint64_t launches = 0;
     uint64_t launches_per_step = 0;
@@ -799,6 +802,21 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     return FGB_OK;
 }
 
+// Uploads and downloads run as kernels that read and write the caller's arrays
+// where the device addresses pageable memory through the host's page tables
+// (Grace's coherent link); elsewhere, or with FGB_HOST_IO=staged, the host packs
+// into pinned staging buffers that the copy engines move.  Both give the same bytes.
+static bool host_io_direct() {
+    const char *e = getenv("FGB_HOST_IO");
+    if (e && strcmp(e, "staged") == 0) return false;
+    int dev = 0, pageable = 0, host_tables = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+        return false;
+    return pageable && host_tables;
+}
+
 static int batch_init(fgb_batch *b) {
     fgb_solver *s = b->solver;
     const fgb_params &p = s->params;
@@ -905,6 +923,11 @@ static int batch_init(fgb_batch *b) {
     FGB_CUDA(cudaStreamSynchronize(st), "batch init");
     b->ids.assign(b->n_scenes, {});
     b->ids_stale.assign(b->n_scenes, 0);
+    b->direct = host_io_direct();
+    if (b->direct) {
+        FGB_CUDA(b->obst_dev.alloc(b->n_scenes), "batch alloc");
+        FGB_CUDA(b->st_count.ensure(1), "batch alloc");
+    }
     b->scene_tris.assign(b->n_scenes, {});
     return FGB_OK;
 }
@@ -933,12 +956,45 @@ static int sync_ids(fgb_batch *b) {
     return FGB_OK;
 }
 
+// What every upload ends with: the scene table learns whether the scene holds
+// obstacles, and the scene's key prefix is set in case a surface call precedes
+// the first step.
+static void upload_done(fgb_batch *b, uint32_t k, uint32_t obstacles) {
+    if (b->h_scenes[k].obstacles != obstacles) {
+        b->h_scenes[k].obstacles = obstacles;
+        b->tris_dirty = true;  // re-uploads the scene table before the next step
+    }
+    launch_fill_u32(b->keys_sorted.p + b->first[k], b->counts[k], b->mbits >= 32 ? 0u : (k << b->mbits), b->stream());
+}
+
+// One kernel reads the caller's arrays and writes the scene segment (ids go to
+// ids_dev, which is then the only copy).  Returns once the kernel has finished,
+// so the caller may reuse its arrays.
+static int batch_upload_direct(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
+    const uint64_t n = xs->n, f = b->first[k];
+    const int c = b->cur;
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemsetAsync(b->obst_dev.p + k, 0, sizeof(uint32_t), st), "upload");
+    const HostParticlesIn in{xs->position, xs->velocity, xs->mass, xs->type, xs->colour, xs->id};
+    launch_pack_from_host(in, n, b->x[c].p + f, b->v[c].p + f, b->type[c].p + f, b->col[c].p + f, b->slot[c].p + f,
+                          b->ids_dev.p + f, b->obst_dev.p + k, st);
+    FGB_CUDA(cudaGetLastError(), "upload kernel");
+    FGB_CUDA(cudaMemcpyAsync(b->st_count.p, b->obst_dev.p + k, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+             "upload");
+    FGB_CUDA(cudaStreamSynchronize(st), "upload sync");
+    b->ids[k].clear();
+    b->ids_stale[k] = 0;
+    upload_done(b, k, b->st_count.p[0]);
+    return FGB_OK;
+}
+
 static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     if (k >= b->n_scenes) return fail(FGB_ERR_INVALID, "upload: scene out of range");
     if (!xs || xs->n != b->counts[k]) return fail(FGB_ERR_INVALID, "upload: particle count differs from the batch");
     const uint64_t n = xs->n, f = b->first[k];
     if (n && (!xs->position || !xs->velocity || !xs->mass || !xs->type))
         return fail(FGB_ERR_INVALID, "upload: null particle array");
+    if (b->direct) return batch_upload_direct(b, k, xs);
     FGB_CUDA(b->st_x.ensure(n), "upload staging");
     FGB_CUDA(b->st_v.ensure(n), "upload staging");
     FGB_CUDA(b->st_type.ensure(n), "upload staging");
@@ -981,13 +1037,7 @@ static int batch_upload(fgb_batch *b, uint32_t k, const fgb_particles *xs) {
     // consumer asks for them (sync_ids)
     launch_iota_u32(b->slot[c].p + f, n, st);
     b->ids_stale[k] = 1;
-    const uint32_t obstacles = obstacle_count.load();
-    if (b->h_scenes[k].obstacles != obstacles) {
-        b->h_scenes[k].obstacles = obstacles;
-        b->tris_dirty = true;  // re-uploads the scene table before the next step
-    }
-    // the scene's key prefix, in case a surface call precedes the first step
-    launch_fill_u32(b->keys_sorted.p + f, n, b->mbits >= 32 ? 0u : (k << b->mbits), st);
+    upload_done(b, k, obstacle_count.load());
     // the staging buffers are only rewritten after a synchronisation (the next
     // upload's, or a download's), so the copies may still be running on return
     return FGB_OK;
@@ -1030,7 +1080,15 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
                  "copy_scene");
         launch_fill_u32(dst->keys_sorted.p + fd, n, dst->mbits >= 32 ? 0u : (dk << dst->mbits), st);
     }
-    dst->ids[dk] = src->ids[sk];
+    if (src->direct && !dst->direct) {  // dst keeps its ids on the host
+        dst->ids[dk].assign(n, 0);
+        if (n)
+            FGB_CUDA(cudaMemcpyAsync(dst->ids[dk].data(), src->ids_dev.p + fs, n * sizeof(uint64_t),
+                                     cudaMemcpyDeviceToHost, st),
+                     "copy_scene ids");
+    } else {
+        dst->ids[dk] = src->ids[sk];
+    }
     if (dst->scene_tris[dk].size() != src->scene_tris[sk].size() ||
         (!src->scene_tris[sk].empty() && memcmp(dst->scene_tris[dk].data(), src->scene_tris[sk].data(),
                                                 src->scene_tris[sk].size() * sizeof(TriDev)) != 0)) {
@@ -1065,6 +1123,16 @@ static int batch_download(fgb_batch *b, uint32_t k, fgb_particles *xs) {
     if (k >= b->n_scenes) return fail(FGB_ERR_INVALID, "download: scene out of range");
     if (!xs || xs->n != b->counts[k]) return fail(FGB_ERR_INVALID, "download: particle count differs");
     const uint64_t n = xs->n, f = b->first[k];
+    if (b->direct) {
+        const int c = b->cur;
+        cudaStream_t st = b->stream();
+        const HostParticlesOut out{xs->position, xs->velocity, xs->mass, xs->type, xs->colour, xs->id};
+        launch_unpack_to_host(out, n, b->x[c].p + f, b->v[c].p + f, b->type[c].p + f, b->col[c].p + f,
+                              b->slot[c].p + f, b->ids_dev.p + f, st);
+        FGB_CUDA(cudaGetLastError(), "download kernel");
+        FGB_CUDA(cudaStreamSynchronize(st), "download sync");
+        return FGB_OK;
+    }
     FGB_CUDA(b->st_x.ensure(n), "download staging");
     FGB_CUDA(b->st_v.ensure(n), "download staging");
     FGB_CUDA(b->st_type.ensure(n), "download staging");
@@ -1420,6 +1488,12 @@ int fgb_batch_sync(fgb_batch *b) {
     return FGB_OK;
 }
 
+int fgb_batch_host_io(const fgb_batch *b, int *direct) {
+    if (!b || !direct) return fail(FGB_ERR_INVALID, "host_io: bad argument");
+    *direct = b->direct ? 1 : 0;
+    return FGB_OK;
+}
+
 int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
     if (!b || !flags) return fail(FGB_ERR_INVALID, "error_flags: bad argument");
     cudaStream_t st = b->stream();
@@ -1656,9 +1730,9 @@ int fgb_batch_sources_drains(fgb_batch *b, uint32_t k, const fgb_source *sources
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
     b->graphs_ok = false;
-    // the scene's ids by its new slots, for downloads
-    b->ids[k].assign(counts[k], 0);
-    if (counts[k])
+    // the scene's ids by its new slots, for staged downloads
+    b->ids[k].assign(b->direct ? 0 : counts[k], 0);
+    if (counts[k] && !b->direct)
         FGB_CUDA(cudaMemcpyAsync(b->ids[k].data(), b->ids_dev.p + first[k], counts[k] * sizeof(uint64_t),
                                  cudaMemcpyDeviceToHost, st),
                  "sources_drains ids");

@@ -194,6 +194,12 @@ class Batch:
         capi.check(self.lib.fgb_batch_grid_info(self._h, k, ctypes.byref(gi)))
         return gi
 
+    def host_io_direct(self):
+        """True where uploads and downloads are kernels on the caller's arrays."""
+        d = ctypes.c_int()
+        capi.check(self.lib.fgb_batch_host_io(self._h, ctypes.byref(d)))
+        return bool(d.value)
+
     def error_flags(self):
         f = ctypes.c_uint32()
         capi.check(self.lib.fgb_batch_error_flags(self._h, ctypes.byref(f)))
