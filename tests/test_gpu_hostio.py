@@ -153,3 +153,33 @@ def test_advance_direct_equals_staged(monkeypatch):
     monkeypatch.delenv("FGB_HOST_IO", raising=False)
     _same(results[0][0], results[1][0])
     assert results[0][1] == results[1][1]
+
+
+def test_download_into_fresh_mappings(monkeypatch):
+    """Output arrays on pages the host never wrote (fresh anonymous mappings) get
+    every element written, as with reused arrays."""
+    import mmap
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = _scene((17, 13, 11), 411)
+    solver = SphSolver(params=params)
+    b = _batch(monkeypatch, solver, [(scenes.copy_particles(parts), cfg)], staged=False)
+    _require_direct(b)
+    b.step(2)
+    want = b.download(0)
+    n = len(parts["mass"])
+    maps = []
+
+    def fresh(count, dt):
+        m = mmap.mmap(-1, count * np.dtype(dt).itemsize, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
+        maps.append(m)
+        return np.frombuffer(m, dtype=dt, count=count)
+
+    out = {"id": fresh(n, np.uint64), "type": fresh(n, np.int32), "mass": fresh(n, np.float32),
+           "position": fresh(3 * n, np.float32), "velocity": fresh(3 * n, np.float32),
+           "colour": fresh(n, np.uint32)}
+    pv = capi.particles_view(out)
+    capi.check(b.lib.fgb_batch_download(b.handle, 0, ctypes.byref(pv)))
+    _same({k: np.array(v) for k, v in out.items()}, want)
+    del out, pv
+    b.close()
+    solver.close()
