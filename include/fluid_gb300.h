@@ -167,6 +167,11 @@ int fgb_batch_set_colliders(fgb_batch *b, uint32_t scene, const fgb_triangle *tr
 /* Advance every scene of the batch by `steps` steps: one launch per stage for
  * all scenes, replayed from a CUDA graph. Asynchronous on the solver stream. */
 int fgb_batch_step(fgb_batch *b, uint32_t steps);
+/* Upload the scene table and capture, instantiate and upload the step graphs now
+ * instead of in the next fgb_batch_step, so that the first step of a new batch (or
+ * the first after a change of colliders, timing or launch shape) costs a plain
+ * step.  Synchronous; changes no result. */
+int fgb_batch_prepare(fgb_batch *b);
 int fgb_batch_download(fgb_batch *b, uint32_t scene, fgb_particles *xs);
 /* Marching cubes of one scene's current state; synchronous. */
 int fgb_batch_surface(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
@@ -306,6 +311,8 @@ int fgb_serve_fetch(fgb_server *sv, uint64_t ticket, fgb_particles *xs, fgb_mesh
 int fgb_serve_get_stats(fgb_server *sv, fgb_serve_stats *out);
 /* Wall time of every tick (one batched step), in seconds. */
 int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
+/* Particles stepped by every tick, in the order of fgb_serve_step_latencies. */
+int fgb_serve_tick_particles(fgb_server *sv, uint64_t *out, uint64_t max, uint64_t *count);
 int fgb_serve_drain(fgb_server *sv, double timeout_seconds);
 int fgb_serve_destroy(fgb_server *sv);
 

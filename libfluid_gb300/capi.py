@@ -207,6 +207,7 @@ _SIGS = {
     "fgb_batch_sync": (ctypes.c_int, [c_void_p]),
     "fgb_batch_error_flags": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
     "fgb_batch_host_io": (ctypes.c_int, [c_void_p, P(ctypes.c_int)]),
+    "fgb_batch_prepare": (ctypes.c_int, [c_void_p]),
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),
     "fgb_batch_set_timing": (ctypes.c_int, [c_void_p, ctypes.c_int]),
     "fgb_batch_autotune": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(TuneResult)]),
@@ -225,6 +226,8 @@ _SIGS = {
     "fgb_serve_fetch": (ctypes.c_int, [c_void_p, ctypes.c_uint64, P(Particles), P(Mesh)]),
     "fgb_serve_get_stats": (ctypes.c_int, [c_void_p, P(ServeStats)]),
     "fgb_serve_step_latencies": (ctypes.c_int, [c_void_p, P(ctypes.c_double), ctypes.c_uint64,
+                                                P(ctypes.c_uint64)]),
+    "fgb_serve_tick_particles": (ctypes.c_int, [c_void_p, P(ctypes.c_uint64), ctypes.c_uint64,
                                                 P(ctypes.c_uint64)]),
     "fgb_serve_drain": (ctypes.c_int, [c_void_p, ctypes.c_double]),
     "fgb_serve_destroy": (ctypes.c_int, [c_void_p]),

@@ -62,23 +62,108 @@ namespace {
 
 constexpr float kPi = 3.14159265358979323846f;
 
+// Device blocks of one solver's batches, kept for reuse instead of freed.  Every
+// batch of a solver queues its work on the solver's stream, so a block handed back
+// while kernels that use it are still queued can go to the next allocation of the
+// same solver without a wait: that allocation's users queue behind them
+// (fgb_set_stream drains the old stream before it switches).  cudaMalloc and the
+// device-wide synchronisation of cudaFree cost ~1.6 and ~1.8 ms for the ~40 arrays
+// of a batch, and the serving loop rebuilds a group of scenes several times a
+// second.  Blocks come in size classes (four per power of two above 64 KiB) so that
+// batches of similar sizes reuse each other's blocks.
+class DevPool {
+  public:
+    ~DevPool() { trim(); }
+    static size_t size_class(size_t bytes) {
+        if (bytes <= 65536) return (bytes + 511) & ~size_t(511);
+        size_t top = 65536;
+        while (top * 2 < bytes) top *= 2;  // top < bytes <= 2 top
+        const size_t quarter = top / 4;
+        return top + (bytes - top + quarter - 1) / quarter * quarter;
+    }
+    void *get(size_t bytes, cudaError_t *e) {
+        const size_t c = size_class(bytes);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto it = free_.find(c);
+            if (it != free_.end()) {
+                void *p = it->second;
+                free_.erase(it);
+                cached_ -= c;
+                *e = cudaSuccess;
+                return p;
+            }
+        }
+        void *p = nullptr;
+        *e = cudaMalloc(&p, c);
+        if (*e == cudaErrorMemoryAllocation) {  // give the cached blocks back and retry
+            (void)cudaGetLastError();
+            trim();
+            *e = cudaMalloc(&p, c);
+        }
+        return *e == cudaSuccess ? p : nullptr;
+    }
+    void put(void *p, size_t bytes) {
+        const size_t c = size_class(bytes);
+        std::lock_guard<std::mutex> lk(mu_);
+        free_.emplace(c, p);
+        cached_ += c;
+    }
+    void trim() {
+        std::lock_guard<std::mutex> lk(mu_);
+        for (auto &f : free_) cudaFree(f.second);
+        free_.clear();
+        cached_ = 0;
+    }
+    size_t cached_bytes() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return cached_;
+    }
+
+  private:
+    std::mutex mu_;
+    std::multimap<size_t, void *> free_;
+    size_t cached_ = 0;
+};
+
+// The pool that Dev::alloc draws from on this thread (none: cudaMalloc); set by
+// PoolScope in the batch functions that allocate.  A block goes back to the pool
+// it came from.
+thread_local DevPool *t_pool = nullptr;
+struct PoolScope {
+    DevPool *prev;
+    explicit PoolScope(DevPool *p) : prev(t_pool) { t_pool = p; }
+    ~PoolScope() { t_pool = prev; }
+};
+
 template <class T>
 struct Dev {
     T *p = nullptr;
     size_t n = 0;
+    DevPool *pool = nullptr;
     Dev() = default;
     Dev(const Dev &) = delete;
     Dev &operator=(const Dev &) = delete;
     ~Dev() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (pool) pool->put(p, n * sizeof(T));
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
+        pool = nullptr;
     }
     cudaError_t alloc(size_t count) {
         release();
         if (count == 0) count = 1;
-        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        cudaError_t e;
+        if (t_pool) {
+            p = (T *)t_pool->get(count * sizeof(T), &e);
+            if (e == cudaSuccess) pool = t_pool;
+        } else {
+            e = cudaMalloc((void **)&p, count * sizeof(T));
+        }
         if (e == cudaSuccess) n = count;
         else p = nullptr;
         return e;
@@ -86,6 +171,7 @@ struct Dev {
     void swap(Dev &o) {
         std::swap(p, o.p);
         std::swap(n, o.n);
+        std::swap(pool, o.pool);
     }
 };
 
@@ -340,6 +426,7 @@ static uint32_t tune_bucket(int32_t profile, uint64_t n) {
 }
 
 struct fgb_solver {
+    DevPool pool;  // first member: outlives every block its batches hand back
     fgb_params params;
     Phys ph;
     cudaStream_t own = nullptr;
@@ -631,6 +718,7 @@ struct fgb_batch {
 
     int sync_tris() {
         if (!tris_dirty) return FGB_OK;
+        PoolScope scope(&solver->pool);
         std::vector<TriDev> all;
         for (uint32_t k = 0; k < n_scenes; ++k) {
             h_scenes[k].tri_first = (uint32_t)all.size();
@@ -679,6 +767,20 @@ struct fgb_batch {
         return FGB_OK;
     }
 
+    // Everything the first step would set up: the scene table and the two step
+    // graphs, instantiated and uploaded to the device.
+    int prepare() {
+        int rc = sync_tris();
+        if (rc) return rc;
+        if (!graphs_ok) {
+            rc = build_graphs();
+            if (rc) return rc;
+            for (auto &g : graph) FGB_CUDA(cudaGraphUpload(g, stream()), "graph upload");
+        }
+        FGB_CUDA(cudaStreamSynchronize(stream()), "prepare sync");
+        return FGB_OK;
+    }
+
     int step(uint32_t steps) {
         int rc = sync_tris();
         if (rc) return rc;
@@ -696,6 +798,7 @@ struct fgb_batch {
 
     int ensure_surface() {
         if (surf_ready) return FGB_OK;
+        PoolScope scope(&solver->pool);
         FGB_CUDA(mc_keys.alloc(n), "surface alloc");
         FGB_CUDA(mc_vals.alloc(n), "surface alloc");
         FGB_CUDA(mc_xs.alloc(n), "surface alloc");
@@ -772,6 +875,7 @@ struct fgb_batch {
 
     int surface_emit(uint64_t tri_total) {
         if (tri_total > tris_out.n || !tris_out.p) {
+            PoolScope scope(&solver->pool);
             uint64_t cap = std::max<uint64_t>(tri_total + tri_total / 4, 1024);
             FGB_CUDA(tris_out.alloc(cap), "surface: triangles alloc");
         }
@@ -805,6 +909,7 @@ static int mesh_assign(fgb_mesh *m, const fgb_mesh_triangle *dev, uint64_t count
 // The per-particle arrays a step rebuilds (sort keys, p*, lists, lambda, ...), for
 // `cap` particles; their contents do not outlive a step.
 static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
+    PoolScope scope(&b->solver->pool);
     const fgb_params &p = b->solver->params;
     for (int c = 0; c < 2; ++c) FGB_CUDA(b->ps[c].alloc(cap), "batch alloc");
     FGB_CUDA(b->keys_in.alloc(cap), "batch alloc");
@@ -856,6 +961,7 @@ static bool host_io_direct() {
 }
 
 static int batch_init(fgb_batch *b) {
+    PoolScope scope(&b->solver->pool);
     fgb_solver *s = b->solver;
     const fgb_params &p = s->params;
     b->ph = s->ph;
@@ -1373,6 +1479,9 @@ int fgb_set_stream(fgb_solver *s, void *cuda_stream) {
     if (!s) return fail(FGB_ERR_INVALID, "set_stream: null solver");
     cudaStream_t st = cuda_stream ? (cudaStream_t)cuda_stream : s->own;
     if (st == s->stream) return FGB_OK;
+    // blocks in the solver's pool may still be in use by work queued on the old
+    // stream; the new stream's work must not overtake it
+    FGB_CUDA(cudaStreamSynchronize(s->stream), "set_stream sync");
     s->stream = st;
     if (s->cached) {
         for (auto &g : s->cached->graph)
@@ -1509,6 +1618,7 @@ int batch_resident(fgb_batch *b, uint32_t k, ResidentScene *out) {
 }
 
 void *batch_wire_scratch(fgb_batch *b, uint64_t bytes) {
+    PoolScope scope(&b->solver->pool);
     if (b->wire.n < bytes && b->wire.alloc(bytes) != cudaSuccess) return nullptr;
     return b->wire.p;
 }
@@ -1526,6 +1636,11 @@ int fgb_batch_sync(fgb_batch *b) {
     if (!b) return fail(FGB_ERR_INVALID, "sync: null batch");
     FGB_CUDA(cudaStreamSynchronize(b->stream()), "sync");
     return FGB_OK;
+}
+
+int fgb_batch_prepare(fgb_batch *b) {
+    if (!b) return fail(FGB_ERR_INVALID, "prepare: null batch");
+    return b->prepare();
 }
 
 int fgb_batch_host_io(const fgb_batch *b, int *direct) {
@@ -1629,6 +1744,7 @@ int fgb_batch_sources_drains(fgb_batch *b, uint32_t k, const fgb_source *sources
     if (!b || !count || k >= b->n_scenes) return fail(FGB_ERR_INVALID, "sources_drains: bad argument");
     if ((n_sources && !sources) || (n_drains && !drains)) return fail(FGB_ERR_INVALID, "sources_drains: null array");
     const fgb_config &c = b->cfg[k];
+    PoolScope scope(&b->solver->pool);
     // emission (oclsph.hpp:678-691), with the drain test of 694-705 applied to the
     // new particles right away, as the reference erases after emitting
     const float spacing = (b->solver->params.h * c.scale / 2);

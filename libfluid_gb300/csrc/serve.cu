@@ -99,6 +99,7 @@ struct fgb_server {
     uint64_t ticks = 0, particle_steps = 0, completed = 0, rejected = 0, failed = 0, rebuilds = 0;
     double busy = 0, rebuild_time = 0;
     std::vector<double> step_latency;
+    std::vector<uint64_t> step_particles;  // particles of each tick, beside step_latency
     std::string last_error;
 
     double t() const { return now_s() - t0; }
@@ -176,6 +177,12 @@ struct fgb_server {
                     return rc;
                 }
             }
+            // graph capture and the scene table belong to the rebuild, not the next tick
+            int rc2 = fgb_batch_prepare(nb);
+            if (rc2) {
+                fgb_batch_destroy(nb);
+                return rc2;
+            }
         }
         if (g.batch) fgb_batch_destroy(g.batch);
         g.batch = nb;
@@ -248,7 +255,10 @@ struct fgb_server {
         step_latency.push_back(s1 - s0);
         busy += s1 - s0;
         ticks++;
-        for (Request *r : g.scenes) particle_steps += r->n;
+        uint64_t tick_n = 0;
+        for (Request *r : g.scenes) tick_n += r->n;
+        particle_steps += tick_n;
+        step_particles.push_back(tick_n);
         for (Request *r : done) {
             r->status = FGB_SERVE_DONE;
             r->t_done = t();
@@ -430,6 +440,14 @@ int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t
     std::lock_guard<std::mutex> lk(sv->mu);
     *count = sv->step_latency.size();
     for (uint64_t i = 0; out && i < max && i < sv->step_latency.size(); ++i) out[i] = sv->step_latency[i];
+    return FGB_OK;
+}
+
+int fgb_serve_tick_particles(fgb_server *sv, uint64_t *out, uint64_t max, uint64_t *count) {
+    if (!sv || !count) return fail(FGB_ERR_INVALID, "serve_tick_particles: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->step_particles.size();
+    for (uint64_t i = 0; out && i < max && i < sv->step_particles.size(); ++i) out[i] = sv->step_particles[i];
     return FGB_OK;
 }
 

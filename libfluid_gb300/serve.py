@@ -66,6 +66,14 @@ class Server:
         capi.check(self.lib.fgb_serve_step_latencies(self._h, buf, cnt.value, ctypes.byref(cnt)))
         return np.frombuffer(buf, dtype=np.float64)[:cnt.value].copy()
 
+    def tick_particles(self):
+        """Particles stepped by each tick, aligned with step_latencies()."""
+        cnt = ctypes.c_uint64()
+        capi.check(self.lib.fgb_serve_tick_particles(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_uint64 * max(cnt.value, 1))()
+        capi.check(self.lib.fgb_serve_tick_particles(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        return np.frombuffer(buf, dtype=np.uint64)[:cnt.value].copy()
+
     def close(self):
         if self._h:
             self.lib.fgb_serve_destroy(self._h)
