@@ -313,6 +313,8 @@ int fgb_serve_get_stats(fgb_server *sv, fgb_serve_stats *out);
 int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
 /* Particles stepped by every tick, in the order of fgb_serve_step_latencies. */
 int fgb_serve_tick_particles(fgb_server *sv, uint64_t *out, uint64_t max, uint64_t *count);
+/* Start of every tick in seconds since fgb_serve_create, in the same order. */
+int fgb_serve_tick_starts(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
 int fgb_serve_drain(fgb_server *sv, double timeout_seconds);
 int fgb_serve_destroy(fgb_server *sv);
 

@@ -229,6 +229,8 @@ _SIGS = {
                                                 P(ctypes.c_uint64)]),
     "fgb_serve_tick_particles": (ctypes.c_int, [c_void_p, P(ctypes.c_uint64), ctypes.c_uint64,
                                                 P(ctypes.c_uint64)]),
+    "fgb_serve_tick_starts": (ctypes.c_int, [c_void_p, P(ctypes.c_double), ctypes.c_uint64,
+                                             P(ctypes.c_uint64)]),
     "fgb_serve_drain": (ctypes.c_int, [c_void_p, ctypes.c_double]),
     "fgb_serve_destroy": (ctypes.c_int, [c_void_p]),
     "fgb_exclusive_scan_u32_noalloc": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p]),

@@ -3,14 +3,18 @@
 // Requests (a scene, a step count, optionally a final surface) arrive at any time.
 // A worker thread admits waiting requests in arrival order while their device
 // footprint fits the HBM budget and keeps every admitted scene resident on the
-// device.  Admitted scenes are packed first-fit into groups of at most
-// tick_particles particles; one tick advances one group by one step (one launch per
-// stage for all its scenes, fgb_batch_step), taking the groups round robin, so a
-// tick costs about the same whatever the mix.  When a group's membership changes,
-// its survivors are copied device-to-device into a new batch (fgb_batch_copy_scene
-// keeps their particle order, so a scene's result is bit-identical alone and in any
-// mix).  Finished scenes optionally run marching cubes, their final state is copied
-// to the host, and their memory is released.
+// device.  Admitted scenes are spread over groups of at most tick_particles
+// particles; one tick advances one group by one step (one launch per stage for all
+// its scenes, fgb_batch_step), taking the groups round robin.  A tick's latency is
+// linear in its particles (~0.27 ms + 2.9 ns a particle on GB300), so the groups are
+// kept as few and as even as the scenes allow: a new scene joins the lightest group
+// it fits, and when the groups drift apart (the heaviest above 1.5x the lightest, or
+// more groups than ceil(total / tick_particles) need) the scenes are re-spread
+// largest first onto the lightest group (LPT).  When a group's membership changes,
+// its scenes are copied device-to-device into a new batch from wherever they live
+// (fgb_batch_copy_scene keeps their particle order, so a scene's result is
+// bit-identical alone and in any mix).  Finished scenes optionally run marching
+// cubes, their final state is copied to the host, and their memory is released.
 //
 // Budget accounting: rebuilding a group holds its old and new batch at once, so
 // admission keeps the sum of active footprints within half the budget.
@@ -100,6 +104,7 @@ struct fgb_server {
     double busy = 0, rebuild_time = 0;
     std::vector<double> step_latency;
     std::vector<uint64_t> step_particles;  // particles of each tick, beside step_latency
+    std::vector<double> step_start;        // start of each tick, seconds since creation
     std::string last_error;
 
     double t() const { return now_s() - t0; }
@@ -130,28 +135,116 @@ struct fgb_server {
         return fresh;
     }
 
-    // First group with room for r (particles, and scene-id bits above the Morton
-    // key), else a new group.
-    void place(Request *r) {
-        for (auto &g : groups) {
-            if (opt.one_at_a_time && !g->want.empty()) continue;
-            if (!g->want.empty() && g->particles + r->n > opt.tick_particles) continue;
-            const uint32_t mb = std::max(g->mbits, r->mbits);
-            if (mb + bits_of((uint32_t)g->want.size()) > 32) continue;
-            g->want.push_back(r);
-            g->particles += r->n;
-            g->mbits = mb;
-            return;
-        }
-        auto g = std::make_unique<ServeGroup>();
-        g->want.push_back(r);
-        g->particles = r->n;
-        g->mbits = r->mbits;
-        groups.push_back(std::move(g));
+    // Whether r may join a group of `particles` particles, `count` scenes and Morton
+    // width `mbits` (room in the tick, and scene-id bits above the Morton key).
+    bool fits(uint64_t particles, size_t count, uint32_t mbits, const Request *r) const {
+        if (!count) return true;
+        if (opt.one_at_a_time) return false;
+        if (particles + r->n > opt.tick_particles) return false;
+        return std::max(mbits, r->mbits) + bits_of((uint32_t)count) <= 32;
     }
 
-    // Make g.batch hold exactly g.want; survivors move on the device.
-    int rebuild(ServeGroup &g) {
+    // The lightest group with room for r, else a new group.
+    void place(Request *r) {
+        ServeGroup *best = nullptr;
+        for (auto &g : groups)
+            if (!g->want.empty() && fits(g->particles, g->want.size(), g->mbits, r) &&
+                (!best || g->particles < best->particles))
+                best = g.get();
+        if (!best) {
+            groups.push_back(std::make_unique<ServeGroup>());
+            best = groups.back().get();
+        }
+        best->want.push_back(r);
+        best->particles += r->n;
+        best->mbits = std::max(best->mbits, r->mbits);
+    }
+
+    // Re-spread the scenes when the groups drift apart (see the top of the file).
+    void rebalance() {
+        if (opt.one_at_a_time) return;
+        std::vector<ServeGroup *> used;
+        uint64_t total = 0, lo = ~0ull, hi = 0;
+        for (auto &g : groups)
+            if (!g->want.empty()) {
+                used.push_back(g.get());
+                total += g->particles;
+                lo = std::min(lo, g->particles);
+                hi = std::max(hi, g->particles);
+            }
+        if (used.size() < 2) return;
+        const uint64_t need = (total + opt.tick_particles - 1) / opt.tick_particles;
+        if (used.size() <= need && 2 * hi <= 3 * lo) return;
+        // LPT: largest scene first, onto the lightest group it fits
+        std::vector<Request *> all;
+        for (ServeGroup *g : used) all.insert(all.end(), g->want.begin(), g->want.end());
+        std::sort(all.begin(), all.end(), [](const Request *a, const Request *b) {
+            return a->n != b->n ? a->n > b->n : a->ticket < b->ticket;
+        });
+        struct Bin {
+            std::vector<Request *> scenes;
+            uint64_t particles = 0;
+            uint32_t mbits = 0;
+        };
+        std::vector<Bin> bins(std::max<uint64_t>(need, 1));
+        for (Request *r : all) {
+            Bin *best = nullptr;
+            for (Bin &b : bins)
+                if (fits(b.particles, b.scenes.size(), b.mbits, r) && (!best || b.particles < best->particles))
+                    best = &b;
+            if (!best) {
+                bins.emplace_back();
+                best = &bins.back();
+            }
+            best->scenes.push_back(r);
+            best->particles += r->n;
+            best->mbits = std::max(best->mbits, r->mbits);
+        }
+        // each bin goes to the old group it shares the most particles with, so that
+        // as many groups as possible keep their batch
+        std::vector<bool> taken(used.size(), false);
+        std::vector<ServeGroup *> owner(bins.size(), nullptr);
+        for (size_t b = 0; b < bins.size(); ++b) {
+            uint64_t best_shared = 0;
+            for (size_t g = 0; g < used.size(); ++g) {
+                if (taken[g]) continue;
+                uint64_t shared = 0;
+                for (Request *r : bins[b].scenes)
+                    if (std::find(used[g]->want.begin(), used[g]->want.end(), r) != used[g]->want.end()) shared += r->n;
+                if (shared > best_shared) best_shared = shared, owner[b] = used[g];
+            }
+            if (owner[b]) taken[std::find(used.begin(), used.end(), owner[b]) - used.begin()] = true;
+        }
+        for (size_t g = 0; g < used.size(); ++g)
+            if (!taken[g]) {
+                used[g]->want.clear();
+                used[g]->particles = 0;
+                used[g]->mbits = 0;
+            }
+        for (size_t b = 0; b < bins.size(); ++b) {
+            ServeGroup *g = owner[b];
+            if (!g) {
+                groups.push_back(std::make_unique<ServeGroup>());
+                g = groups.back().get();
+            }
+            // the same scenes in another order need no rebuild
+            std::vector<Request *> a = bins[b].scenes, c = g->scenes;
+            std::sort(a.begin(), a.end());
+            std::sort(c.begin(), c.end());
+            g->want = a == c ? g->scenes : bins[b].scenes;
+            g->particles = bins[b].particles;
+            g->mbits = bins[b].mbits;
+        }
+    }
+
+    // Make g.batch hold exactly g.want; scenes already resident (in any group's
+    // current batch, found through `where`) move on the device.  The old batch is
+    // handed to `retired`: other groups' rebuilds may still copy from it.
+    struct Home {
+        fgb_batch *batch;
+        uint32_t scene;
+    };
+    int rebuild(ServeGroup &g, const std::map<Request *, Home> &where, std::vector<fgb_batch *> &retired) {
         const double r0 = now_s();
         fgb_batch *nb = nullptr;
         if (!g.want.empty()) {
@@ -165,9 +258,9 @@ struct fgb_server {
             if (rc) return rc;
             for (size_t k = 0; k < g.want.size(); ++k) {
                 Request *r = g.want[k];
-                auto it = std::find(g.scenes.begin(), g.scenes.end(), r);
-                if (it != g.scenes.end()) {
-                    rc = fgb_batch_copy_scene(nb, (uint32_t)k, g.batch, (uint32_t)(it - g.scenes.begin()));
+                auto it = where.find(r);
+                if (it != where.end()) {
+                    rc = fgb_batch_copy_scene(nb, (uint32_t)k, it->second.batch, it->second.scene);
                 } else {
                     fgb_particles v = r->view();
                     rc = fgb_batch_upload(nb, (uint32_t)k, &v);
@@ -184,7 +277,7 @@ struct fgb_server {
                 return rc2;
             }
         }
-        if (g.batch) fgb_batch_destroy(g.batch);
+        if (g.batch) retired.push_back(g.batch);
         g.batch = nb;
         g.scenes = g.want;
         std::lock_guard<std::mutex> lk(mu);
@@ -253,6 +346,7 @@ struct fgb_server {
         }
         std::lock_guard<std::mutex> lk(mu);
         step_latency.push_back(s1 - s0);
+        step_start.push_back(s0 - t0);
         busy += s1 - s0;
         ticks++;
         uint64_t tick_n = 0;
@@ -285,21 +379,29 @@ struct fgb_server {
                 fresh = admit();
             }
             for (Request *r : fresh) place(r);
-            // drop empty groups, then bring the changed ones up to date
-            std::vector<std::unique_ptr<ServeGroup>> kept;
-            for (auto &g : groups) {
-                if (g->want.empty()) {
-                    if (g->batch) fgb_batch_destroy(g->batch);
-                    continue;
-                }
-                kept.push_back(std::move(g));
-            }
-            groups.swap(kept);
+            rebalance();
+            // bring the changed groups up to date (scenes move between batches on the
+            // device), then release the batches nothing uses any more
+            std::map<Request *, Home> where;
+            for (auto &g : groups)
+                for (size_t k = 0; k < g->scenes.size(); ++k) where[g->scenes[k]] = Home{g->batch, (uint32_t)k};
+            std::vector<fgb_batch *> retired;
             for (auto &g : groups)
                 if (g->want != g->scenes) {
-                    const int rc = rebuild(*g);
-                    if (rc) fail_group(*g, rc);
+                    const int rc = rebuild(*g, where, retired);
+                    if (rc) {
+                        // the old batch may still hold scenes that other groups copy
+                        if (g->batch) retired.push_back(g->batch);
+                        g->batch = nullptr;
+                        g->scenes.clear();
+                        fail_group(*g, rc);
+                    }
                 }
+            for (fgb_batch *b : retired) fgb_batch_destroy(b);
+            std::vector<std::unique_ptr<ServeGroup>> kept;
+            for (auto &g : groups)
+                if (!g->want.empty()) kept.push_back(std::move(g));
+            groups.swap(kept);
             // round robin over the groups that hold scenes
             ServeGroup *pick = nullptr;
             for (size_t i = 0; i < groups.size() && !pick; ++i) {
@@ -448,6 +550,14 @@ int fgb_serve_tick_particles(fgb_server *sv, uint64_t *out, uint64_t max, uint64
     std::lock_guard<std::mutex> lk(sv->mu);
     *count = sv->step_particles.size();
     for (uint64_t i = 0; out && i < max && i < sv->step_particles.size(); ++i) out[i] = sv->step_particles[i];
+    return FGB_OK;
+}
+
+int fgb_serve_tick_starts(fgb_server *sv, double *out, uint64_t max, uint64_t *count) {
+    if (!sv || !count) return fail(FGB_ERR_INVALID, "serve_tick_starts: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->step_start.size();
+    for (uint64_t i = 0; out && i < max && i < sv->step_start.size(); ++i) out[i] = sv->step_start[i];
     return FGB_OK;
 }
 

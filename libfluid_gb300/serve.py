@@ -74,6 +74,14 @@ class Server:
         capi.check(self.lib.fgb_serve_tick_particles(self._h, buf, cnt.value, ctypes.byref(cnt)))
         return np.frombuffer(buf, dtype=np.uint64)[:cnt.value].copy()
 
+    def tick_starts(self):
+        """Start of each tick, seconds since the server was created."""
+        cnt = ctypes.c_uint64()
+        capi.check(self.lib.fgb_serve_tick_starts(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_double * max(cnt.value, 1))()
+        capi.check(self.lib.fgb_serve_tick_starts(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        return np.frombuffer(buf, dtype=np.float64)[:cnt.value].copy()
+
     def close(self):
         if self._h:
             self.lib.fgb_serve_destroy(self._h)
