@@ -218,6 +218,7 @@ int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count
 #define FGB_PROBE_LIST_COUNT  8 /* u16 neighbour-list length per particle (0xffff: overflow) */
 #define FGB_PROBE_LIST_VALID  9 /* u8 per particle: 1 if its list served the last vorticity pass */
 #define FGB_PROBE_DISPLACEMENT 10 /* f32 distance moved since the grid was built (last delta) */
+#define FGB_PROBE_NEAR_ROW    11 /* u8 per particle: 1 if the last lambda pass ran over the build pass's near row */
 int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes);
 int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes);
 /* Grid geometry of a scene: minimum extent (solver units), cell extent,

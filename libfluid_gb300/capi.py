@@ -37,6 +37,7 @@ PROBE_CUBE_CASES = 7
 PROBE_LIST_COUNT = 8
 PROBE_LIST_VALID = 9
 PROBE_DISPLACEMENT = 10
+PROBE_NEAR_ROW = 11
 
 f3 = ctypes.c_float * 3
 

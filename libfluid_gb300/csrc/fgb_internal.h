@@ -72,6 +72,11 @@ struct StepView {
     uint32_t *hlist;       // n * hcap
     uint16_t *hcount;      // entries per particle (kListOverflow: use nlist / the cells)
     uint32_t hcap;
+    // near rows: the build pass's hit row keeps every candidate within h + near_skin;
+    // near[a] = 1 while particle a's row is that row (null: near rows off)
+    uint8_t *near;
+    float near_r2;         // (h + near_skin)^2, rounded up
+    float near_skin;
 };
 
 constexpr uint16_t kListOverflow = 0xffffu;

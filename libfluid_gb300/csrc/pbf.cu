@@ -156,6 +156,8 @@ struct GatherArgs {
     uint32_t *hlist;
     uint16_t *hcount;
     uint32_t hcap;
+    uint8_t *near;  // null: no near rows
+    float near_r2, near_skin;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -182,14 +184,17 @@ __device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t
 }
 
 // Whether particle a may use its list for the current positions.
+// mcd: the 27 cells' maximum displacement when the caller already has it, else < 0.
 template <int MODE>
-__device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key) {
+__device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
+                                         float mcd = -1.f) {
     if (A.cap == 0 || MODE == kBuild) return false;
     const uint16_t c = A.ncount[a];
     if (c == kListOverflow) return false;
     if (MODE == kFresh) return true;
     if (MODE == kStored) return A.valid[a] != 0;
-    const bool ok = A.disp[a] + max_cell_disp(S, A.cellmax, key, A.mbits) <= A.skin;
+    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+    const bool ok = A.disp[a] + mcd <= A.skin;
     A.valid[a] = ok ? 1 : 0;
     return ok;
 }
@@ -284,6 +289,16 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 // still applies its own range tests to each hit, so its sums are bit-identical to a
 // walk.  A row that overflows (count > hcap) sends its passes back to the candidates.
 // Rows are particle-major like the Verlet lists.
+//
+// Near rows.  The build pass (the step's first lambda pass) keeps in the hit row
+// every candidate within h + near_skin of the grid positions rather than within h,
+// and marks the row (near[a]).  By the same bound as the Verlet lists, that row still
+// holds every neighbour within h while disp_a + max disp_b <= near_skin, so a later
+// lambda pass for which the bound holds runs its arithmetic straight over the row,
+// without the range-filter phase, and leaves the row for the delta pass after it.
+// The extra entries (~15% at 0.05 h) fail the passes' own range tests, so the sums
+// are unchanged.  A pass for which the bound fails filters as before and clears the
+// mark: the row it writes holds the hits of that pass's positions only.
 struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
@@ -343,7 +358,6 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     const uint32_t key = A.keys[a];
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
-    const bool list = use_list<MODE>(A, S, a, key);
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
     auto body = [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
@@ -377,24 +391,40 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             }
         }
     };
-    if (A.hcap == 0 && MODE != kBuild) {
-        for_candidates(A, S, a, key, list, ps, body);
-    } else {
-        // phase 1: range filter (and the Verlet list on the build pass)
-        RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
-        HitWriter hits(A, a);
-        for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
-            const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
-            const bool in = PROFILE == kRef ? sqrtf(r2) <= ph.h : r2 <= ph.hh;
-            if (in) hits.add(b);
-        });
-        if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
-        hits.close(A, a);
-        // phase 2: the kernel arithmetic over the hits, in walk order
-        if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, ps, body);
-        else for_candidates(A, S, a, key, list, ps, body);
+    // a later pass whose near row still holds every neighbour iterates it directly
+    float mcd = -1.f;
+    bool done = false;
+    if (MODE != kBuild && A.near) {
+        if (A.near[a] && have_hits(A, a)) {
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+            done = A.disp[a] + mcd <= A.near_skin;
+        }
+        if (done) for_hits(A, a, ps, body);
+        else A.near[a] = 0;
+    }
+    if (!done) {
+        const bool list = use_list<MODE>(A, S, a, key, mcd);
+        if (A.hcap == 0 && MODE != kBuild) {
+            for_candidates(A, S, a, key, list, ps, body);
+        } else {
+            // phase 1: range filter (and the Verlet list on the build pass)
+            RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
+            HitWriter hits(A, a);
+            const bool near_row = MODE == kBuild && A.near;
+            for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+                const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
+                const bool in = near_row ? r2 <= A.near_r2 : PROFILE == kRef ? sqrtf(r2) <= ph.h : r2 <= ph.hh;
+                if (in) hits.add(b);
+            });
+            if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
+            hits.close(A, a);
+            if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
+            // phase 2: the kernel arithmetic over the hits, in walk order
+            if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, ps, body);
+            else for_candidates(A, S, a, key, list, ps, body);
+        }
     }
     float dens, lam;
     if (PROFILE == kRef) {
@@ -873,6 +903,10 @@ GatherArgs gather_args(const StepView &s) {
     A.hlist = s.hlist;
     A.hcount = s.hcount;
     A.hcap = s.hlist ? s.hcap : 0;
+    // near rows need the displacement bound (Verlet lists) and hit rows
+    A.near = s.cap && A.hcap ? s.near : nullptr;
+    A.near_r2 = s.near_r2;
+    A.near_skin = s.near_skin;
     return A;
 }
 

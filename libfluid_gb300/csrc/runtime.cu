@@ -489,6 +489,8 @@ struct fgb_batch {
     uint32_t hit_cap = 64;
     uint32_t list_cap = 96;
     float skin_frac = 0.2f;
+    float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
+    Dev<uint8_t> near;
     int block = 128;  // threads per CTA of the gather kernels
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
@@ -581,6 +583,11 @@ struct fgb_batch {
         s.hlist = hlist.p;
         s.hcount = hcount.p;
         s.hcap = hlist.p ? hit_cap : 0;
+        const float near_skin = near_frac * ph.h;
+        const float near_reach = (ph.h + near_skin) * 1.00001f;
+        s.near = near_frac > 0.f ? near.p : nullptr;
+        s.near_r2 = near_reach * near_reach;
+        s.near_skin = near_skin;
         return s;
     }
 
@@ -929,6 +936,7 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
         FGB_CUDA(b->hlist.alloc(cap * b->hit_cap), "batch alloc hit lists");
         FGB_CUDA(b->hcount.alloc(cap), "batch alloc");
     }
+    if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
@@ -1041,6 +1049,7 @@ static int batch_init(fgb_batch *b) {
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
     if (b->list_cap) FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
     if (const char *e = getenv("FGB_HIT_CAP")) b->hit_cap = (uint32_t)atoi(e);
+    if (const char *e = getenv("FGB_NEAR_SKIN")) b->near_frac = (float)atof(e);
     if (b->hit_cap > 4096) b->hit_cap = 4096;
     b->hit_cap = (b->hit_cap + 3u) & ~3u;  // rows move as 16-byte vectors
     int rc = alloc_step_arrays(b, n);
@@ -1695,6 +1704,7 @@ int fgb_batch_probe_size(fgb_batch *b, uint32_t what, uint64_t *bytes) {
     case FGB_PROBE_LIST_COUNT: *bytes = n * 2; break;
     case FGB_PROBE_LIST_VALID: *bytes = n; break;
     case FGB_PROBE_DISPLACEMENT: *bytes = n * 4; break;
+    case FGB_PROBE_NEAR_ROW: *bytes = n; break;
     default: return fail(FGB_ERR_INVALID, "probe: unknown array");
     }
     return FGB_OK;
@@ -1717,6 +1727,7 @@ int fgb_batch_probe(fgb_batch *b, uint32_t what, void *host_out, uint64_t bytes)
     case FGB_PROBE_LIST_COUNT: src = b->ncount.p; break;
     case FGB_PROBE_LIST_VALID: src = b->valid.p; break;
     case FGB_PROBE_DISPLACEMENT: src = b->disp.p; break;
+    case FGB_PROBE_NEAR_ROW: src = b->near.p; break;
     }
     if (!src) return fail(FGB_ERR_INVALID, "probe: array not allocated yet");
     cudaStream_t st = b->stream();
