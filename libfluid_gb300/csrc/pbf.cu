@@ -297,8 +297,9 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 // lambda pass for which the bound holds runs its arithmetic straight over the row,
 // without the range-filter phase, and leaves the row for the delta pass after it.
 // The extra entries (~15% at 0.05 h) fail the passes' own range tests, so the sums
-// are unchanged.  A pass for which the bound fails filters as before and clears the
-// mark: the row it writes holds the hits of that pass's positions only.
+// are unchanged.  A pass for which the bound fails (for any lane of the warp) filters
+// as before and clears the mark: the row it writes holds the hits of that pass's
+// positions only.
 struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
@@ -391,14 +392,18 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             }
         }
     };
-    // a later pass whose near row still holds every neighbour iterates it directly
+    // a later pass whose near row still holds every neighbour iterates it directly;
+    // the choice is made per warp (all lanes or none), as a warp that mixed the two
+    // paths would run both one after the other
     float mcd = -1.f;
     bool done = false;
     if (MODE != kBuild && A.near) {
+        bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
             mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
-            done = A.disp[a] + mcd <= A.near_skin;
+            ok = A.disp[a] + mcd <= A.near_skin;
         }
+        done = __all_sync(__activemask(), ok);
         if (done) for_hits(A, a, ps, body);
         else A.near[a] = 0;
     }

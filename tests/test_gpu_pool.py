@@ -81,3 +81,4 @@ def test_batch_grows_within_the_pool():
     b.close()
     solver.close()
     _same(got, _alone(params, edited, cfg, 2))
+
