@@ -651,7 +651,21 @@ __global__ void __launch_bounds__(256)
     const uint32_t key = A.keys[a];
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
-    const bool list = use_list<kCheck>(A, S, a, key);
+    // the near row, while its bound still holds for the whole warp, serves this pass
+    // and the apply pass (it holds obstacles and candidates beyond h, which both
+    // passes' own tests skip); near[a] stays set to tell the apply pass
+    float mcd = -1.f;
+    bool near = false;
+    if (A.near) {
+        bool ok = false;
+        if (A.near[a] && have_hits(A, a)) {
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+            ok = A.disp[a] + mcd <= A.near_skin;
+        }
+        near = __all_sync(__activemask(), ok);
+        if (!near) A.near[a] = 0;
+    }
+    const bool list = near ? false : use_list<kCheck>(A, S, a, key, mcd);
     const float va[3] = {va4.x, va4.y, va4.z};
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
     // fluid_known: b came from the hit list, which holds fluid particles only
@@ -679,7 +693,9 @@ __global__ void __launch_bounds__(256)
         }
     };
     auto any = [&](uint32_t b, const float4 &pb) { body(b, pb, false); };
-    if (A.hcap == 0) {
+    if (near) {
+        for_hits(A, a, ps, any);
+    } else if (A.hcap == 0) {
         for_candidates(A, S, a, key, list, ps, any);
     } else {
         // phase 1: fluid candidates within h; phase 2: the arithmetic over them
@@ -733,7 +749,9 @@ __global__ void __launch_bounds__(256)
         e[2] = __fmaf_rn(sc, d[2], e[2]);
     };
     if (have_hits(A, a)) {
-        for_hits(A, a, ps, [&](uint32_t b, const float4 &pb) { body(b, pb, true); });
+        // a near row (still marked) holds obstacles too; a filtered row fluid only
+        const bool fluid_rows = !(A.near && A.near[a]);
+        for_hits(A, a, ps, [&](uint32_t b, const float4 &pb) { body(b, pb, fluid_rows); });
     } else {
         for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), ps,
                        [&](uint32_t b, const float4 &pb) { body(b, pb, false); });
