@@ -242,6 +242,58 @@ def bench_batched(params, steps=20, mc_every=10, tune=True):
                     "advance loop: one drop-in solver per scene, advance() with host arrays every frame"}
 
 
+def bench_large(params, steps=20, warmup=3, tune=True):
+    """The 8 388 608-particle double dam break (two 128x128x256 blocks): its p* array
+    (134 MB) is larger than L2, so it is the case where HBM traffic is real.  Device-
+    resident steps with CUDA events on the solver stream; the whole step's algorithmic
+    bytes (N x (384 + 60 I) = 624 B per particle-step at I = 4) over its duration."""
+    import torch
+    from libfluid_gb300 import scenes
+    from libfluid_gb300.solver import Batch, SphSolver
+    parts, cfg = scenes.double_dam_8m()
+    n = len(parts["mass"])
+    solver = SphSolver(params=params)
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    tuned = None
+    if tune:
+        t = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+        tuned = t.autotune(3)
+        t.close()
+    batch = Batch(solver, [(parts, cfg)])
+    batch.set_timing(True)
+    batch.step(warmup)
+    batch.sync()
+    names = stage_names(cfg.iterations)
+    stage_sum = [0.0] * len(names)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            batch.step(1)
+            e1.record(stream)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        for i, v in enumerate(batch.stage_times()):
+            stage_sum[i] += v
+    flags = batch.error_flags()
+    batch.close()
+    solver.close()
+    ms = total_ms / steps
+    stages = {}
+    for name, v in zip(names, stage_sum):
+        stages[name] = round(stages.get(name, 0.0) + v / steps, 4)
+    peak, peak_kind = measured_peaks()
+    algo = n * (384 + 60 * int(cfg.iterations))
+    gbs = algo / (ms * 1e-3) / 1e9
+    return {"workload": "double_dam_8m", "particles": n, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3), "stages_ms_per_step": stages,
+            "step_algorithmic_bytes": algo, "step_achieved_gbs": gbs, "hbm_peak_gbs": peak,
+            "hbm_peak_kind": peak_kind, "step_hbm_frac": gbs / peak, "error_flags": flags,
+            "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3)} if tuned else None)}
+
+
 def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=0):
     """Workload 5: saturation throughput, then a Poisson stream at 80% of it."""
     import numpy as np
@@ -463,9 +515,10 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_seconds, params, scenes.dam_break_1m)
-    batched = serving = None
+    batched = serving = large = None
     if world == 1 and not args.no_extra:
         batched = bench_batched(params, tune=not args.no_tune)
+        large = bench_large(params, tune=not args.no_tune)
         serving = bench_serving(params)
 
     if rank == 0:
@@ -496,6 +549,7 @@ def run_ours(args):
             "error_flags": flags,
             "batched": batched,
             "serving": serving,
+            "large": large,
         }
         print(json.dumps(line), flush=True)
     batch.close()
