@@ -252,6 +252,42 @@ __device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint3
     }
 }
 
+// for_row with a second per-candidate value gathered beside each position (the
+// delta pass's lambda_b, the vorticity passes' v_b and |omega_b|): the four values
+// load together with the four positions, ahead of the arithmetic, instead of inside
+// it after the range test.  f(b, p_b, get) with get() returning the value.
+template <bool kSameKernel = false, class T, class F>
+__device__ __forceinline__ void for_row_x(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
+                                          const float4 *__restrict__ ps, const T *__restrict__ ex, F &f) {
+    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
+    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
+    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
+    uint32_t j = 0;
+    for (; j + 4 <= c; j += 4) {
+        const uint4 b = next;
+        if (j + 4 < c) next = load(j + 4);
+        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
+        const T e0 = __ldg(&ex[b.x]), e1 = __ldg(&ex[b.y]), e2 = __ldg(&ex[b.z]), e3 = __ldg(&ex[b.w]);
+        f(b.x, p0, [&] { return e0; });
+        f(b.y, p1, [&] { return e1; });
+        f(b.z, p2, [&] { return e2; });
+        f(b.w, p3, [&] { return e3; });
+    }
+    if (j < c) {
+        const uint4 b = next;
+        const uint32_t rest = c - j;
+        const float4 p0 = __ldg(&ps[b.x]);
+        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
+        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
+        const T e0 = __ldg(&ex[b.x]);
+        const T e1 = rest > 1 ? __ldg(&ex[b.y]) : e0;
+        const T e2 = rest > 2 ? __ldg(&ex[b.z]) : e0;
+        f(b.x, p0, [&] { return e0; });
+        if (rest > 1) f(b.y, p1, [&] { return e1; });
+        if (rest > 2) f(b.z, p2, [&] { return e2; });
+    }
+}
+
 template <class F>
 __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
                                                bool list, const float4 *__restrict__ ps, F &&f) {
@@ -535,7 +571,8 @@ __global__ void __launch_bounds__(256)
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float la = lambda[a];
     float px = 0.f, py = 0.f, pz = 0.f;
-    auto body = [&](uint32_t b, const float4 &pb) {
+    // lam_b() is lambda of b (gathered beside p_b on rows, loaded on demand on walks)
+    auto body = [&](uint32_t b, const float4 &pb, auto lam_b) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
@@ -546,7 +583,7 @@ __global__ void __launch_bounds__(256)
                 w = ph.poly6f * (t * t * t);
             }
             const float corr = -ph.corr_k * corr_pow(w / ph.corr_ref, ph.corr_n);
-            const float factor = (la + __ldg(&lambda[b]) + corr) / ph.rho0;
+            const float factor = (la + lam_b() + corr) / ph.rho0;
             if (r >= kKernelEpsilon && r <= ph.h) {
                 const float hr = ph.h - r;
                 const float sc = ph.spikyf * ((hr * hr) / r);
@@ -561,7 +598,7 @@ __global__ void __launch_bounds__(256)
                     const float t = ph.hh - r2;
                     const float corr = -ph.corr_k * corr_pow((t * t * t) / ph.corr_wdq, ph.corr_n);
                     const float hr = ph.h - r;
-                    const float sc = pb.w * ((hr * hr) / r) * (la + __ldg(&lambda[b]) + corr);
+                    const float sc = pb.w * ((hr * hr) / r) * (la + lam_b() + corr);
                     px = __fmaf_rn(sc, dx, px);
                     py = __fmaf_rn(sc, dy, py);
                     pz = __fmaf_rn(sc, dz, pz);
@@ -570,9 +607,11 @@ __global__ void __launch_bounds__(256)
         }
     };
     if (have_hits(A, a)) {
-        for_hits(A, a, ps_in, body);
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps_in, lambda, body);
     } else {
-        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), ps_in, body);
+        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), ps_in, [&](uint32_t b, const float4 &pb) {
+            body(b, pb, [&] { return __ldg(&lambda[b]); });
+        });
     }
     float world[3];
     if (PROFILE == kRef) {
@@ -668,13 +707,14 @@ __global__ void __launch_bounds__(256)
     const bool list = near ? false : use_list<kCheck>(A, S, a, key, mcd);
     const float va[3] = {va4.x, va4.y, va4.z};
     float o[3] = {0.f, 0.f, 0.f}, xs[3] = {0.f, 0.f, 0.f};
-    // fluid_known: b came from the hit list, which holds fluid particles only
-    auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
+    // fluid_known: b came from a filtered hit row, which holds fluid particles only;
+    // vel_b() is v of b (gathered beside p_b on rows, loaded on demand on walks)
+    auto body = [&](uint32_t b, const float4 &pb, auto vel_b, bool fluid_known) {
         if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         if (!(r2 <= ph.hh)) return;
-        const float4 vb = __ldg(&v[b]);
+        const float4 vb = vel_b();
         const float vab[3] = {vb.x - va[0], vb.y - va[1], vb.z - va[2]};
         const float t = ph.hh - r2;
         const float mw = pb.w * (t * t * t);
@@ -692,9 +732,12 @@ __global__ void __launch_bounds__(256)
             o[2] = __fmaf_rn(sc, cr[2], o[2]);
         }
     };
-    auto any = [&](uint32_t b, const float4 &pb) { body(b, pb, false); };
+    auto any = [&](uint32_t b, const float4 &pb) {
+        body(b, pb, [&] { return __ldg(&v[b]); }, false);
+    };
     if (near) {
-        for_hits(A, a, ps, any);
+        auto any_row = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, false); };
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps, v, any_row);
     } else if (A.hcap == 0) {
         for_candidates(A, S, a, key, list, ps, any);
     } else {
@@ -707,8 +750,8 @@ __global__ void __launch_bounds__(256)
         });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
-            auto fluid = [&](uint32_t b, const float4 &pb) { body(b, pb, true); };
-            for_row<true>(A.hlist, A.hcap, a, hits.count, ps, fluid);
+            auto fluid = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, true); };
+            for_row_x<true>(A.hlist, A.hcap, a, hits.count, ps, v, fluid);
         } else {
             for_candidates(A, S, a, key, list, ps, any);
         }
@@ -734,8 +777,9 @@ __global__ void __launch_bounds__(256)
     const float4 pa = ps[a];
     const float4 oa = omega[a];
     float e[3] = {0.f, 0.f, 0.f};
-    // fluid_known: b came from the hit list, which holds fluid particles only
-    auto body = [&](uint32_t b, const float4 &pb, bool fluid_known) {
+    // fluid_known: b came from a filtered hit row, which holds fluid particles only;
+    // om_b() is omega of b (gathered beside p_b on rows, loaded on demand on walks)
+    auto body = [&](uint32_t b, const float4 &pb, auto om_b, bool fluid_known) {
         if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -743,7 +787,7 @@ __global__ void __launch_bounds__(256)
         const float r = sqrtf(r2);
         if (!(r >= kKernelEpsilon)) return;
         const float hr = ph.h - r;
-        const float sc = pb.w * ((hr * hr) / r) * (__ldg(&omega[b].w) - oa.w);
+        const float sc = pb.w * ((hr * hr) / r) * (om_b().w - oa.w);
         e[0] = __fmaf_rn(sc, d[0], e[0]);
         e[1] = __fmaf_rn(sc, d[1], e[1]);
         e[2] = __fmaf_rn(sc, d[2], e[2]);
@@ -751,10 +795,12 @@ __global__ void __launch_bounds__(256)
     if (have_hits(A, a)) {
         // a near row (still marked) holds obstacles too; a filtered row fluid only
         const bool fluid_rows = !(A.near && A.near[a]);
-        for_hits(A, a, ps, [&](uint32_t b, const float4 &pb) { body(b, pb, fluid_rows); });
+        auto row = [&](uint32_t b, const float4 &pb, auto om_b) { body(b, pb, om_b, fluid_rows); };
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps, omega, row);
     } else {
-        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), ps,
-                       [&](uint32_t b, const float4 &pb) { body(b, pb, false); });
+        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), ps, [&](uint32_t b, const float4 &pb) {
+            body(b, pb, [&] { return __ldg(&omega[b]); }, false);
+        });
     }
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ex = e[0] * gs, ey = e[1] * gs, ez = e[2] * gs;
