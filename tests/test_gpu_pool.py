@@ -82,3 +82,20 @@ def test_batch_grows_within_the_pool():
     solver.close()
     _same(got, _alone(params, edited, cfg, 2))
 
+
+
+def test_prepare_changes_no_result():
+    """fgb_batch_prepare (graphs and scene table set up ahead of the first step)."""
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = scenes.cube_scene(30000, 71)
+    solver = SphSolver(params=params)
+    a = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+    b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+    capi.check(b.lib.fgb_batch_prepare(b.handle))
+    capi.check(b.lib.fgb_batch_prepare(b.handle))  # a second call is a no-op
+    a.step(3)
+    b.step(3)
+    _same(a.download(0), b.download(0))
+    a.close()
+    b.close()
+    solver.close()

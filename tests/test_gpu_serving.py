@@ -42,6 +42,14 @@ def _serve(solver, reqs, one_at_a_time=False, stagger=0.0, tick_particles=0):
     results = [sv.fetch(t) for t in tickets]
     st = sv.stats()
     lat = sv.step_latencies()
+    # per-tick particles and start times line up with the latencies
+    tp, t0 = sv.tick_particles(), sv.tick_starts()
+    assert len(tp) == len(lat) == len(t0) == st.ticks
+    assert int(tp.sum()) == st.particle_steps
+    assert (np.diff(t0) >= 0).all() and (t0 >= 0).all()
+    if tick_particles:
+        sizes = [len(p["mass"]) for p, _, _, _ in reqs]
+        assert int(tp.max()) <= max(tick_particles, max(sizes))
     sv.close()
     return results, st, lat
 
@@ -104,4 +112,24 @@ def test_over_budget_request_is_rejected_and_others_complete():
     with pytest.raises(capi.FluidError):
         sv.fetch(t_big)
     sv.close()
+    solver.close()
+
+
+def test_groups_spread_evenly_and_scenes_move_between_batches():
+    """Many small scenes under a small tick budget: lightest-fit placement and the
+    re-spread move resident scenes between group batches on the device; every result
+    still equals the scene advanced alone."""
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    reqs = []
+    for i, (n, steps) in enumerate([(13824, 9), (4096, 3), (13824, 12), (8000, 5), (4096, 8), (13824, 4),
+                                    (8000, 10), (4096, 6)]):
+        parts, cfg = scenes.cube_scene(n, 800 + i)
+        reqs.append((parts, cfg, steps, False))
+    res, st, lat = _serve(solver, reqs, stagger=0.001, tick_particles=30000)
+    assert st.completed == len(reqs) and st.failed == 0
+    assert st.rebuilds > 0
+    for (parts, cfg, steps, _), (got, _) in zip(reqs, res):
+        ref, _ = _alone(solver, parts, cfg, steps, False)
+        for f in ("id", "position", "velocity", "colour"):
+            assert (got[f] == ref[f]).all(), f
     solver.close()
