@@ -148,6 +148,9 @@ void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, flo
 void launch_unpack_to_host(const HostParticlesOut &out, uint64_t n, const float4 *x, const float4 *v,
                            const int32_t *type, const uint32_t *col, const uint32_t *slot, const uint64_t *ids,
                            cudaStream_t st);
+// type, colour, id and mass (from p*.w) only: final once a step's grid is built
+void launch_unpack_static(const HostParticlesOut &out, uint64_t n, const float4 *ps_grid, const int32_t *type,
+                          const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st);
 
 // vertex welding of device-resident triangles (weld.cu)
 int weld_device(const fgb_mesh_triangle *d_tris, uint64_t n_tris, uint32_t *d_index, float *d_vertices,

@@ -12,6 +12,8 @@
 // warp access to host memory is a contiguous run of 4-byte words.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "fgb_internal.h"
 
 namespace fgb {
@@ -96,7 +98,36 @@ __global__ void __launch_bounds__(kTile) k_unpack_to_host(HostParticlesOut out, 
     }
 }
 
+// The fields of a download that are final once the step's grid is built (the
+// particles' sorted order): type, colour, id, and mass (carried in p*.w).  Runs on a
+// second stream while the step's gathers run; positions and velocities follow at
+// the end of the step (k_unpack_to_host with only those two set).
+__global__ void __launch_bounds__(kTile) k_unpack_static(HostParticlesOut out, uint64_t n,
+                                                        const float4 *__restrict__ ps_grid,
+                                                        const int32_t *__restrict__ type,
+                                                        const uint32_t *__restrict__ col,
+                                                        const uint32_t *__restrict__ slot,
+                                                        const uint64_t *__restrict__ ids) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (out.mass) out.mass[i] = ps_grid[i].w;
+        if (out.type) out.type[i] = type[i];
+        if (out.colour) out.colour[i] = col[i];
+        if (out.id) {
+            const uint32_t sl = slot[i];
+            out.id[i] = sl < n ? ids[sl] : sl;
+        }
+    }
+}
+
 }  // namespace
+
+void launch_unpack_static(const HostParticlesOut &out, uint64_t n, const float4 *ps_grid, const int32_t *type,
+                          const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st) {
+    // a quarter of the SMs: the stores only need to be in flight, and the gathers
+    // that run beside them keep the rest
+    unsigned g = (unsigned)std::min<uint64_t>((n + kTile - 1) / kTile, 38u * 2u);
+    if (n) k_unpack_static<<<g ? g : 1u, kTile, 0, st>>>(out, n, ps_grid, type, col, slot, ids);
+}
 
 void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
                            uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st) {

@@ -469,6 +469,11 @@ struct fgb_batch {
     std::vector<uint8_t> ids_stale;  // per scene: ids_dev not yet given the last upload's ids (sync_ids)
     bool direct = false;    // uploads and downloads address the caller's arrays from kernels (hostio.cu)
     Dev<uint32_t> obst_dev; // per scene: obstacle count of the last direct upload
+    // direct downloads of fgb_advance: the step graphs record grid_ready once the
+    // grid is built, and io_stream writes the fields final from then on (type,
+    // colour, id, mass) while the gathers run
+    cudaEvent_t grid_ready = nullptr, io_done = nullptr;
+    cudaStream_t io_stream = nullptr;
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -532,6 +537,12 @@ struct fgb_batch {
             if (g) cudaGraphExecDestroy(g);
         for (auto &ev : events) cudaEventDestroy(ev);
         for (auto &ev : piece_events) cudaEventDestroy(ev);
+        if (io_stream) {
+            cudaStreamSynchronize(io_stream);
+            cudaStreamDestroy(io_stream);
+        }
+        if (grid_ready) cudaEventDestroy(grid_ready);
+        if (io_done) cudaEventDestroy(io_done);
     }
 
     cudaStream_t stream() const { return solver->stream; }
@@ -626,6 +637,7 @@ struct fgb_batch {
             launch_diffuse(s, colour_sums.p, colour_count.p, st);
             l += 2;
         }
+        if (grid_ready) FGB_CUDA(cudaEventRecordWithFlags(grid_ready, st, cudaEventRecordExternal), "grid event");
         mark(k, st);
         // p* of the grid stays in ps_grid; the iterations ping-pong between ps[0] and ps[1]
         const float4 *pin = ps_grid.p;
@@ -1080,6 +1092,9 @@ static int batch_init(fgb_batch *b) {
     if (b->direct) {
         FGB_CUDA(b->obst_dev.alloc(b->n_scenes), "batch alloc");
         FGB_CUDA(b->st_count.ensure(1), "batch alloc");
+        FGB_CUDA(cudaEventCreateWithFlags(&b->grid_ready, cudaEventDisableTiming), "batch events");
+        FGB_CUDA(cudaEventCreateWithFlags(&b->io_done, cudaEventDisableTiming), "batch events");
+        FGB_CUDA(cudaStreamCreateWithFlags(&b->io_stream, cudaStreamNonBlocking), "batch stream");
     }
     b->scene_tris.assign(b->n_scenes, {});
     return FGB_OK;
@@ -1959,13 +1974,40 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     if (rc) return rc;
     rc = batch_upload(b, 0, xs);
     if (rc) return rc;
+    const int next = b->cur ^ 1;  // the state set the step writes
     rc = b->step(1);
     if (rc) return rc;
+    if (!b->direct || !b->grid_ready) {
+        if (cfg->surface && mesh_out) {
+            rc = fgb_batch_surface(b, 0, mesh_out);
+            if (rc) return rc;
+        }
+        return batch_download(b, 0, xs);
+    }
+    // direct: while the step runs, the host readies the output pages and io_stream
+    // writes the fields that are final once the grid is built; positions and
+    // velocities follow the step
+    const uint64_t n = xs->n;
+    prefault_outputs({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
+                      {xs->colour, 4 * n}, {xs->id, 8 * n}});
+    const HostParticlesOut fixed{nullptr, nullptr, xs->mass, xs->type, xs->colour, xs->id};
+    FGB_CUDA(cudaStreamWaitEvent(b->io_stream, b->grid_ready, 0), "advance: io wait");
+    launch_unpack_static(fixed, n, b->ps_grid.p, b->type[next].p, b->col[next].p, b->slot[next].p, b->ids_dev.p,
+                         b->io_stream);
+    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
+    FGB_CUDA(cudaEventRecord(b->io_done, b->io_stream), "advance: io event");
     if (cfg->surface && mesh_out) {
         rc = fgb_batch_surface(b, 0, mesh_out);
         if (rc) return rc;
     }
-    return batch_download(b, 0, xs);
+    cudaStream_t st = b->stream();
+    const HostParticlesOut motion{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
+    launch_unpack_to_host(motion, n, b->x[b->cur].p, b->v[b->cur].p, b->type[b->cur].p, b->col[b->cur].p,
+                          b->slot[b->cur].p, b->ids_dev.p, st);
+    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
+    FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
+    FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
+    return FGB_OK;
 }
 
 void fgb_mesh_free(fgb_mesh *m) {
