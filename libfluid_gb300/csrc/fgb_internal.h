@@ -148,6 +148,13 @@ void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, flo
 void launch_unpack_to_host(const HostParticlesOut &out, uint64_t n, const float4 *x, const float4 *v,
                            const int32_t *type, const uint32_t *col, const uint32_t *slot, const uint64_t *ids,
                            cudaStream_t st);
+// an upload in two parts: what the prediction and the sort read (positions,
+// velocities, masses, types; obstacles counted into *obstacles) and what only the
+// reorder reads (colours, ids, upload slots)
+void launch_pack_motion(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type,
+                        uint32_t *obstacles, cudaStream_t st);
+void launch_pack_static(const HostParticlesIn &in, uint64_t n, uint32_t *col, uint32_t *slot, uint64_t *ids,
+                        cudaStream_t st);
 // type, colour, id and mass (from p*.w) only: final once a step's grid is built
 void launch_unpack_static(const HostParticlesOut &out, uint64_t n, const float4 *ps_grid, const int32_t *type,
                           const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st);

@@ -98,6 +98,48 @@ __global__ void __launch_bounds__(kTile) k_unpack_to_host(HostParticlesOut out, 
     }
 }
 
+// An upload split by when the step needs each field: positions, velocities, masses
+// and types feed the prediction and the sort (k_pack_motion, which also counts the
+// obstacles into the scene table), colours, ids and upload slots only the reorder
+// after the sort (k_pack_static, on a second stream while the prediction and the sort
+// run).
+__global__ void __launch_bounds__(kTile) k_pack_motion(HostParticlesIn in, uint64_t n, float4 *__restrict__ x,
+                                                      float4 *__restrict__ v, int32_t *__restrict__ type,
+                                                      uint32_t *__restrict__ obstacles) {
+    __shared__ float sp[3 * kTile], sv[3 * kTile];
+    const unsigned t = threadIdx.x;
+    uint32_t obst = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTile; base < n; base += (uint64_t)gridDim.x * kTile) {
+        const uint32_t m = (uint32_t)(n - base < kTile ? n - base : kTile);
+        const float *pp = in.position + 3 * base, *pv = in.velocity + 3 * base;
+        for (uint32_t j = t; j < 3 * m; j += kTile) {
+            sp[j] = pp[j];
+            sv[j] = pv[j];
+        }
+        __syncthreads();
+        if (t < m) {
+            const uint64_t i = base + t;
+            const int32_t ty = in.type[i];
+            x[i] = make_float4(sp[3 * t], sp[3 * t + 1], sp[3 * t + 2], in.mass[i]);
+            v[i] = make_float4(sv[3 * t], sv[3 * t + 1], sv[3 * t + 2], 0.f);
+            type[i] = ty;
+            obst += ty == FGB_TYPE_OBSTACLE;
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o; o >>= 1) obst += __shfl_xor_sync(0xffffffffu, obst, o);
+    if ((t & 31) == 0 && obst) atomicAdd(obstacles, obst);
+}
+
+__global__ void __launch_bounds__(kTile) k_pack_static(HostParticlesIn in, uint64_t n, uint32_t *__restrict__ col,
+                                                      uint32_t *__restrict__ slot, uint64_t *__restrict__ ids) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        col[i] = in.colour ? in.colour[i] : 0xffffffffu;
+        slot[i] = (uint32_t)i;
+        ids[i] = in.id ? in.id[i] : i;
+    }
+}
+
 // The fields of a download that are final once the step's grid is built (the
 // particles' sorted order): type, colour, id, and mass (carried in p*.w).  Runs on a
 // second stream while the step's gathers run; positions and velocities follow at
@@ -127,6 +169,17 @@ void launch_unpack_static(const HostParticlesOut &out, uint64_t n, const float4 
     // that run beside them keep the rest
     unsigned g = (unsigned)std::min<uint64_t>((n + kTile - 1) / kTile, 38u * 2u);
     if (n) k_unpack_static<<<g ? g : 1u, kTile, 0, st>>>(out, n, ps_grid, type, col, slot, ids);
+}
+
+void launch_pack_motion(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type,
+                        uint32_t *obstacles, cudaStream_t st) {
+    if (n) k_pack_motion<<<grid_of(n), kTile, 0, st>>>(in, n, x, v, type, obstacles);
+}
+
+void launch_pack_static(const HostParticlesIn &in, uint64_t n, uint32_t *col, uint32_t *slot, uint64_t *ids,
+                        cudaStream_t st) {
+    unsigned g = (unsigned)std::min<uint64_t>((n + kTile - 1) / kTile, 38u * 2u);
+    if (n) k_pack_static<<<g ? g : 1u, kTile, 0, st>>>(in, n, col, slot, ids);
 }
 
 void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,

@@ -474,6 +474,10 @@ struct fgb_batch {
     // colour, id, mass) while the gathers run
     cudaEvent_t grid_ready = nullptr, io_done = nullptr;
     cudaStream_t io_stream = nullptr;
+    // and the reorder of each step waits for io_up, recorded by the part of an
+    // fgb_advance upload that io_stream does (colours, ids, slots) during the
+    // prediction and the sort
+    cudaEvent_t io_up = nullptr;
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -543,6 +547,7 @@ struct fgb_batch {
         }
         if (grid_ready) cudaEventDestroy(grid_ready);
         if (io_done) cudaEventDestroy(io_done);
+        if (io_up) cudaEventDestroy(io_up);
     }
 
     cudaStream_t stream() const { return solver->stream; }
@@ -629,6 +634,7 @@ struct fgb_batch {
                                          sort_scratch.p, sort_scratch_bytes, st, err.p, &l);
         if (e != cudaSuccess) return fail_cuda(e, "step: radix sort");
         mark(k, st);
+        if (io_up) FGB_CUDA(cudaStreamWaitEvent(st, io_up, cudaEventWaitExternal), "step: upload event");
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
         if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
@@ -1095,6 +1101,8 @@ static int batch_init(fgb_batch *b) {
         FGB_CUDA(cudaEventCreateWithFlags(&b->grid_ready, cudaEventDisableTiming), "batch events");
         FGB_CUDA(cudaEventCreateWithFlags(&b->io_done, cudaEventDisableTiming), "batch events");
         FGB_CUDA(cudaStreamCreateWithFlags(&b->io_stream, cudaStreamNonBlocking), "batch stream");
+        FGB_CUDA(cudaEventCreateWithFlags(&b->io_up, cudaEventDisableTiming), "batch events");
+        FGB_CUDA(cudaEventRecord(b->io_up, b->io_stream), "batch events");  // complete until an advance
     }
     b->scene_tris.assign(b->n_scenes, {});
     return FGB_OK;
@@ -1949,6 +1957,62 @@ int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out) {
     return FGB_OK;
 }
 
+// fgb_advance with direct host I/O: one frame with a single wait at its end.  The
+// upload and the download are split by when the step needs (or finishes) each field:
+//   main stream: positions, velocities, masses, types in (obstacles counted into the
+//                scene table) -> step -> [surface] -> positions, velocities out
+//   io_stream:   colours, ids, slots in (the step's reorder waits for them) ->
+//                after the grid is built: types, colours, ids, masses out
+static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs, fgb_mesh *mesh_out) {
+    const uint64_t n = xs->n;
+    if (!xs->position || !xs->velocity || !xs->mass || !xs->type)
+        return fail(FGB_ERR_INVALID, "advance: null particle array");
+    int rc = b->sync_tris();  // the scene table before the upload counts obstacles into it
+    if (rc) return rc;
+    cudaStream_t st = b->stream(), io = b->io_stream;
+    const int c = b->cur, next = c ^ 1;
+    uint32_t *obstacles = &b->d_scenes.p[0].obstacles;
+    const HostParticlesIn in{xs->position, xs->velocity, xs->mass, xs->type, xs->colour, xs->id};
+    FGB_CUDA(cudaMemsetAsync(obstacles, 0, sizeof(uint32_t), st), "advance: upload");
+    launch_pack_motion(in, n, b->x[c].p, b->v[c].p, b->type[c].p, obstacles, st);
+    FGB_CUDA(cudaGetLastError(), "advance: upload kernel");
+    // the rest follows on io_stream once the link is free, beside the prediction and
+    // the sort
+    FGB_CUDA(cudaEventRecord(b->io_done, st), "advance: upload event");
+    FGB_CUDA(cudaStreamWaitEvent(io, b->io_done, 0), "advance: upload event");
+    launch_pack_static(in, n, b->col[c].p, b->slot[c].p, b->ids_dev.p, io);
+    FGB_CUDA(cudaGetLastError(), "advance: upload kernel");
+    FGB_CUDA(cudaEventRecord(b->io_up, io), "advance: upload event");
+    launch_fill_u32(b->keys_sorted.p, n, 0u, st);  // scene 0's key prefix for the prediction
+    b->ids[0].clear();
+    b->ids_stale[0] = 0;
+    rc = b->step(1);
+    if (rc) return rc;
+    // while the step runs: the host readies the output pages, io_stream writes the
+    // fields that are final once the grid is built
+    prefault_outputs({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
+                      {xs->colour, 4 * n}, {xs->id, 8 * n}});
+    const HostParticlesOut fixed{nullptr, nullptr, xs->mass, xs->type, xs->colour, xs->id};
+    FGB_CUDA(cudaStreamWaitEvent(io, b->grid_ready, 0), "advance: io wait");
+    launch_unpack_static(fixed, n, b->ps_grid.p, b->type[next].p, b->col[next].p, b->slot[next].p, b->ids_dev.p, io);
+    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
+    FGB_CUDA(cudaEventRecord(b->io_done, io), "advance: io event");
+    if (cfg->surface && mesh_out) {
+        rc = fgb_batch_surface(b, 0, mesh_out);
+        if (rc) return rc;
+    }
+    const HostParticlesOut motion{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
+    launch_unpack_to_host(motion, n, b->x[b->cur].p, b->v[b->cur].p, b->type[b->cur].p, b->col[b->cur].p,
+                          b->slot[b->cur].p, b->ids_dev.p, st);
+    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
+    FGB_CUDA(cudaMemcpyAsync(b->st_count.p, obstacles, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+             "advance: obstacle count");
+    FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
+    FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
+    b->h_scenes[0].obstacles = b->st_count.p[0];  // the device table has it already
+    return FGB_OK;
+}
+
 int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const fgb_triangle *colliders,
                 size_t n_colliders, fgb_mesh *mesh_out) {
     if (!s || !cfg || !xs) return fail(FGB_ERR_INVALID, "advance: null argument");
@@ -1972,42 +2036,16 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     fgb_batch *b = s->cached;
     int rc = fgb_batch_set_colliders(b, 0, colliders, n_colliders);
     if (rc) return rc;
+    if (b->direct && b->io_stream) return advance_direct(b, cfg, xs, mesh_out);
     rc = batch_upload(b, 0, xs);
     if (rc) return rc;
-    const int next = b->cur ^ 1;  // the state set the step writes
     rc = b->step(1);
     if (rc) return rc;
-    if (!b->direct || !b->grid_ready) {
-        if (cfg->surface && mesh_out) {
-            rc = fgb_batch_surface(b, 0, mesh_out);
-            if (rc) return rc;
-        }
-        return batch_download(b, 0, xs);
-    }
-    // direct: while the step runs, the host readies the output pages and io_stream
-    // writes the fields that are final once the grid is built; positions and
-    // velocities follow the step
-    const uint64_t n = xs->n;
-    prefault_outputs({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
-                      {xs->colour, 4 * n}, {xs->id, 8 * n}});
-    const HostParticlesOut fixed{nullptr, nullptr, xs->mass, xs->type, xs->colour, xs->id};
-    FGB_CUDA(cudaStreamWaitEvent(b->io_stream, b->grid_ready, 0), "advance: io wait");
-    launch_unpack_static(fixed, n, b->ps_grid.p, b->type[next].p, b->col[next].p, b->slot[next].p, b->ids_dev.p,
-                         b->io_stream);
-    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
-    FGB_CUDA(cudaEventRecord(b->io_done, b->io_stream), "advance: io event");
     if (cfg->surface && mesh_out) {
         rc = fgb_batch_surface(b, 0, mesh_out);
         if (rc) return rc;
     }
-    cudaStream_t st = b->stream();
-    const HostParticlesOut motion{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
-    launch_unpack_to_host(motion, n, b->x[b->cur].p, b->v[b->cur].p, b->type[b->cur].p, b->col[b->cur].p,
-                          b->slot[b->cur].p, b->ids_dev.p, st);
-    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
-    FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
-    FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
-    return FGB_OK;
+    return batch_download(b, 0, xs);
 }
 
 void fgb_mesh_free(fgb_mesh *m) {
