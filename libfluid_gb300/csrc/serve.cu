@@ -8,9 +8,9 @@
 // its scenes, fgb_batch_step), taking the groups round robin.  A tick's latency is
 // linear in its particles (~0.27 ms + 2.9 ns a particle on GB300), so the groups are
 // kept as few and as even as the scenes allow: a new scene joins the lightest group
-// it fits, and when the groups drift apart (the heaviest above 1.5x the lightest, or
-// more groups than ceil(total / tick_particles) need) the scenes are re-spread
-// largest first onto the lightest group (LPT).  When a group's membership changes,
+// it fits, and whenever the groups are uneven (or more than ceil(total /
+// tick_particles) of them exist) the scenes are re-spread largest first onto the
+// lightest group (LPT); a group that ends up with the same scenes keeps its batch.  When a group's membership changes,
 // its scenes are copied device-to-device into a new batch from wherever they live
 // (fgb_batch_copy_scene keeps their particle order, so a scene's result is
 // bit-identical alone and in any mix).  Finished scenes optionally run marching
@@ -160,7 +160,8 @@ struct fgb_server {
         best->mbits = std::max(best->mbits, r->mbits);
     }
 
-    // Re-spread the scenes when the groups drift apart (see the top of the file).
+    // Re-spread the scenes whenever the groups are uneven (see the top of the file);
+    // a group whose scenes stay the same keeps its batch.
     void rebalance() {
         if (opt.one_at_a_time) return;
         std::vector<ServeGroup *> used;
@@ -174,7 +175,7 @@ struct fgb_server {
             }
         if (used.size() < 2) return;
         const uint64_t need = (total + opt.tick_particles - 1) / opt.tick_particles;
-        if (used.size() <= need && 2 * hi <= 3 * lo) return;
+        if (used.size() <= need && hi == lo) return;
         // LPT: largest scene first, onto the lightest group it fits
         std::vector<Request *> all;
         for (ServeGroup *g : used) all.insert(all.end(), g->want.begin(), g->want.end());
