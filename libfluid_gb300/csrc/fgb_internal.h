@@ -30,6 +30,8 @@ cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint32_t *total, uint64_
                      uint64_t scratch_bytes, cudaStream_t stream, uint32_t *err, uint64_t *launches);
 
 // PBF stages (pbf.cu).  Arrays are indexed by particle over the whole batch.
+struct HostParticlesOut;
+
 struct StepView {
     const SceneDev *scenes;
     const WellDev *wells;
@@ -77,6 +79,9 @@ struct StepView {
     uint8_t *near;
     float near_r2;         // (h + near_skin)^2, rounded up
     float near_skin;
+    // the step's last kernel also stores each particle's final position and velocity
+    // into these host arrays (device-resident pointers, null: no host stores)
+    const HostParticlesOut *hout;
 };
 
 constexpr uint16_t kListOverflow = 0xffffu;

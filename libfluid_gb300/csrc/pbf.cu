@@ -554,16 +554,36 @@ __device__ __forceinline__ void collide_sphere(const SceneDev &S, float *pos) {
 }
 
 
+// Final position and velocity of particle a into the caller's arrays (fgb_advance
+// with direct host I/O): the step's last kernel stores them beside its own writes.
+__device__ __forceinline__ void store_host_motion(const HostParticlesOut *__restrict__ hout, uint32_t a,
+                                                  const float4 &xa, const float4 &va) {
+    if (!hout) return;
+    float *pp = hout->position, *pv = hout->velocity;
+    if (pp) {
+        pp[3 * (size_t)a] = xa.x;
+        pp[3 * (size_t)a + 1] = xa.y;
+        pp[3 * (size_t)a + 2] = xa.z;
+    }
+    if (pv) {
+        pv[3 * (size_t)a] = va.x;
+        pv[3 * (size_t)a + 1] = va.y;
+        pv[3 * (size_t)a + 2] = va.z;
+    }
+}
+
 template <int PROFILE, int MODE>
 __global__ void __launch_bounds__(256)
     k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
-            float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last) {
+            float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
+            const HostParticlesOut *__restrict__ hout) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     const float4 pa = ps_in[a];
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         ps_out[a] = pa;
         if (A.cap) A.disp[a] = 0.f;
+        if (PROFILE == kRef && last) store_host_motion(hout, a, x[a], v[a]);
         return;
     }
     const Phys &ph = A.ph;
@@ -661,7 +681,10 @@ __global__ void __launch_bounds__(256)
             }
         }
         v[a] = make_float4(nv[0], nv[1], nv[2], va.w);
-        if (PROFILE == kRef) x[a] = make_float4(nx[0], nx[1], nx[2], xa.w);
+        if (PROFILE == kRef) {
+            x[a] = make_float4(nx[0], nx[1], nx[2], xa.w);
+            store_host_motion(hout, a, x[a], v[a]);
+        }
     }
 }
 
@@ -767,10 +790,14 @@ __global__ void __launch_bounds__(256)
 // Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
 __global__ void __launch_bounds__(256)
     k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
-                      const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x) {
+                      const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
+                      const HostParticlesOut *__restrict__ hout) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
-    if (A.type[a] == FGB_TYPE_OBSTACLE) return;
+    if (A.type[a] == FGB_TYPE_OBSTACLE) {
+        store_host_motion(hout, a, x[a], v[a]);
+        return;
+    }
     const Phys &ph = A.ph;
     const uint32_t key = A.keys[a];
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
@@ -816,10 +843,13 @@ __global__ void __launch_bounds__(256)
     cross3(N, om, f);
     const float4 vxa = vx[a];
     const float ve = ph.vort_eps, dt = S.dt;
-    v[a] = make_float4(__fmaf_rn(dt, f[0] * ve, vxa.x), __fmaf_rn(dt, f[1] * ve, vxa.y),
-                       __fmaf_rn(dt, f[2] * ve, vxa.z), vxa.w);
+    const float4 vn = make_float4(__fmaf_rn(dt, f[0] * ve, vxa.x), __fmaf_rn(dt, f[1] * ve, vxa.y),
+                                  __fmaf_rn(dt, f[2] * ve, vxa.z), vxa.w);
+    v[a] = vn;
     const float4 xa = x[a];
-    x[a] = make_float4(pa.x * S.scale, pa.y * S.scale, pa.z * S.scale, xa.w);
+    const float4 xn = make_float4(pa.x * S.scale, pa.y * S.scale, pa.z * S.scale, xa.w);
+    x[a] = xn;
+    store_host_motion(hout, a, xn, vn);
 }
 
 // Colour diffusion of the ref profile (oclsph_kernel.h:281-303): each fluid particle
@@ -1039,11 +1069,11 @@ void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int it
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
     const int l = last ? 1 : 0;
     if (iteration == 0) {
-        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
-        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     } else {
-        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
-        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l);
+        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     }
 }
 
@@ -1052,7 +1082,7 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
     const unsigned g = grid_for(s.n, s.block);
     k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
     if (between) between();
-    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1);
+    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

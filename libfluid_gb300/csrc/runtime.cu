@@ -478,6 +478,11 @@ struct fgb_batch {
     // fgb_advance upload that io_stream does (colours, ids, slots) during the
     // prediction and the sort
     cudaEvent_t io_up = nullptr;
+    // the batch behind fgb_advance: the step's last kernel stores final positions and
+    // velocities straight into the caller's arrays, named per frame in hout_dev
+    bool advance_io = false;
+    Dev<HostParticlesOut> hout_dev;
+    Pinned<HostParticlesOut> st_hout;
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -604,6 +609,7 @@ struct fgb_batch {
         s.near = near_frac > 0.f ? near.p : nullptr;
         s.near_r2 = near_reach * near_reach;
         s.near_skin = near_skin;
+        s.hout = advance_io ? hout_dev.p : nullptr;
         return s;
     }
 
@@ -1960,7 +1966,8 @@ int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out) {
 // fgb_advance with direct host I/O: one frame with a single wait at its end.  The
 // upload and the download are split by when the step needs (or finishes) each field:
 //   main stream: positions, velocities, masses, types in (obstacles counted into the
-//                scene table) -> step -> [surface] -> positions, velocities out
+//                scene table) -> step, whose last kernel also stores the final
+//                positions and velocities into the caller's arrays -> [surface]
 //   io_stream:   colours, ids, slots in (the step's reorder waits for them) ->
 //                after the grid is built: types, colours, ids, masses out
 static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs, fgb_mesh *mesh_out) {
@@ -1986,12 +1993,16 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
     launch_fill_u32(b->keys_sorted.p, n, 0u, st);  // scene 0's key prefix for the prediction
     b->ids[0].clear();
     b->ids_stale[0] = 0;
-    rc = b->step(1);
-    if (rc) return rc;
-    // while the step runs: the host readies the output pages, io_stream writes the
-    // fields that are final once the grid is built
+    // output pages readied before any kernel of the frame stores into them
     prefault_outputs({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
                       {xs->colour, 4 * n}, {xs->id, 8 * n}});
+    // the step's last kernel stores positions and velocities into the caller's arrays
+    b->st_hout.p[0] = HostParticlesOut{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
+    FGB_CUDA(cudaMemcpyAsync(b->hout_dev.p, b->st_hout.p, sizeof(HostParticlesOut), cudaMemcpyHostToDevice, st),
+             "advance: output arrays");
+    rc = b->step(1);
+    if (rc) return rc;
+    // io_stream writes the fields that are final once the grid is built
     const HostParticlesOut fixed{nullptr, nullptr, xs->mass, xs->type, xs->colour, xs->id};
     FGB_CUDA(cudaStreamWaitEvent(io, b->grid_ready, 0), "advance: io wait");
     launch_unpack_static(fixed, n, b->ps_grid.p, b->type[next].p, b->col[next].p, b->slot[next].p, b->ids_dev.p, io);
@@ -2001,10 +2012,6 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
         rc = fgb_batch_surface(b, 0, mesh_out);
         if (rc) return rc;
     }
-    const HostParticlesOut motion{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
-    launch_unpack_to_host(motion, n, b->x[b->cur].p, b->v[b->cur].p, b->type[b->cur].p, b->col[b->cur].p,
-                          b->slot[b->cur].p, b->ids_dev.p, st);
-    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
     FGB_CUDA(cudaMemcpyAsync(b->st_count.p, obstacles, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
              "advance: obstacle count");
     FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
@@ -2032,11 +2039,19 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
         if (rc) return rc;
         s->cached_n = xs->n;
         s->cached_cfg = *cfg;
+        fgb_batch *nb = s->cached;
+        if (nb->direct) {  // before the first step captures the graphs
+            PoolScope scope(&s->pool);
+            FGB_CUDA(nb->hout_dev.alloc(1), "advance alloc");
+            FGB_CUDA(nb->st_hout.ensure(1), "advance alloc");
+            FGB_CUDA(cudaMemsetAsync(nb->hout_dev.p, 0, sizeof(HostParticlesOut), nb->stream()), "advance alloc");
+            nb->advance_io = true;
+        }
     }
     fgb_batch *b = s->cached;
     int rc = fgb_batch_set_colliders(b, 0, colliders, n_colliders);
     if (rc) return rc;
-    if (b->direct && b->io_stream) return advance_direct(b, cfg, xs, mesh_out);
+    if (b->advance_io && b->io_stream) return advance_direct(b, cfg, xs, mesh_out);
     rc = batch_upload(b, 0, xs);
     if (rc) return rc;
     rc = b->step(1);
