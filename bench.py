@@ -294,6 +294,45 @@ def bench_large(params, steps=20, warmup=3, tune=True):
             "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3)} if tuned else None)}
 
 
+def bench_ref_profile(steps=30, warmup=5, tune=True):
+    """The 1M dam break under the reference's own constants (the profile the C++
+    drop-in uses by default: no XSPH or vorticity, colour diffusion instead), device-
+    resident steps timed with CUDA events on the solver stream."""
+    import torch
+    from libfluid_gb300 import capi, scenes
+    from libfluid_gb300.solver import Batch, SphSolver
+    params = capi.params(capi.PROFILE_REF, 0.1)
+    parts, cfg = scenes.dam_break_1m()
+    n = len(parts["mass"])
+    solver = SphSolver(params=params)
+    stream = torch.cuda.Stream()
+    solver.set_stream(stream.cuda_stream)
+    if tune:
+        t = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+        t.autotune(3)
+        t.close()
+    batch = Batch(solver, [(parts, cfg)])
+    batch.step(warmup)
+    batch.sync()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total = 0.0
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            batch.step(1)
+            e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+    flags = batch.error_flags()
+    batch.close()
+    solver.close()
+    ms = total / steps
+    return {"workload": "dam_break_1m", "profile": "ref", "particles": n, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3), "error_flags": flags}
+
+
 def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=0):
     """Workload 5: saturation throughput, then a Poisson stream at 80% of it."""
     import numpy as np
@@ -515,10 +554,11 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_seconds, params, scenes.dam_break_1m)
-    batched = serving = large = None
+    batched = serving = large = ref_profile = None
     if world == 1 and not args.no_extra:
         batched = bench_batched(params, tune=not args.no_tune)
         large = bench_large(params, tune=not args.no_tune)
+        ref_profile = bench_ref_profile(tune=not args.no_tune)
         serving = bench_serving(params)
 
     if rank == 0:
@@ -550,6 +590,7 @@ def run_ours(args):
             "batched": batched,
             "serving": serving,
             "large": large,
+            "ref_profile": ref_profile,
         }
         print(json.dumps(line), flush=True)
     batch.close()
