@@ -82,6 +82,8 @@ struct StepView {
     // the step's last kernel also stores each particle's final position and velocity
     // into these host arrays (device-resident pointers, null: no host stores)
     const HostParticlesOut *hout;
+    // the build pass counts the Verlet rows [0] and hit rows [1] that overflowed
+    uint32_t *over;
 };
 
 constexpr uint16_t kListOverflow = 0xffffu;

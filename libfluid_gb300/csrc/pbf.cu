@@ -158,6 +158,7 @@ struct GatherArgs {
     uint32_t hcap;
     uint8_t *near;  // null: no near rows
     float near_r2, near_skin;
+    uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -461,6 +462,15 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
+            if (MODE == kBuild && A.over) {  // one atomic per warp, only when rows overflowed
+                const unsigned m = __activemask();
+                const unsigned lo = __ballot_sync(m, A.cap && built.count > A.cap);
+                const unsigned ho = __ballot_sync(m, A.hcap && hits.count > A.hcap);
+                if ((lo | ho) && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+                    if (lo) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
+                    if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
+                }
+            }
             if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
             // phase 2: the kernel arithmetic over the hits, in walk order
             if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, ps, body);
@@ -1006,6 +1016,7 @@ GatherArgs gather_args(const StepView &s) {
     A.near = s.cap && A.hcap ? s.near : nullptr;
     A.near_r2 = s.near_r2;
     A.near_skin = s.near_skin;
+    A.over = s.over;
     return A;
 }
 

@@ -416,6 +416,7 @@ static void prefault_outputs(std::initializer_list<HostSpan> spans) {
 // Pieces of the pipelined upload and download: host packing or unpacking of one
 // piece overlaps the copies of the others.
 static constexpr uint64_t kPieceMin = 1u << 18;
+static constexpr uint32_t kMaxRowCap = 1024;  // Verlet and hit rows, entries per particle
 static constexpr uint32_t kPieces = 4;
 
 // Autotuner cache key: physics profile and floor(log2(particles)).
@@ -439,6 +440,9 @@ struct fgb_solver {
         float skin;
     };
     std::map<uint32_t, Tuned> tuned;
+    // row capacities (Verlet, hit) that batches grew to, per (profile, log2 n) bucket:
+    // later batches of the bucket start there
+    std::map<uint32_t, std::pair<uint32_t, uint32_t>> caps;
     fgb_batch *cached = nullptr;  // single-scene batch behind fgb_advance
     uint64_t cached_n = 0;
     fgb_config cached_cfg{};
@@ -483,6 +487,10 @@ struct fgb_batch {
     bool advance_io = false;
     Dev<HostParticlesOut> hout_dev;
     Pinned<HostParticlesOut> st_hout;
+    // rows that overflowed in each step's build pass, copied to st_over at the end of
+    // the step; grow_rows() enlarges the capacities when more than 1% did
+    Dev<uint32_t> over;
+    Pinned<uint32_t> st_over;
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -610,6 +618,7 @@ struct fgb_batch {
         s.near_r2 = near_reach * near_reach;
         s.near_skin = near_skin;
         s.hout = advance_io ? hout_dev.p : nullptr;
+        s.over = over.p;
         return s;
     }
 
@@ -632,6 +641,7 @@ struct fgb_batch {
         StepView s = view(c);
         uint64_t l = 0;
         uint32_t k = 0;
+        if (over.p) FGB_CUDA(cudaMemsetAsync(over.p, 0, 2 * sizeof(uint32_t), st), "step: overflow counters");
         mark(k, st);
         launch_predict_keys(s, st);
         l += 1;
@@ -667,6 +677,9 @@ struct fgb_batch {
             mark(k, st);
             l += 2;
         }
+        if (over.p)
+            FGB_CUDA(cudaMemcpyAsync(st_over.p, over.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                     "step: overflow counters");
         FGB_CUDA(cudaGetLastError(), "step: launch");
         launches_per_step = l;
         if (timing) n_stages = k ? k - 1 : 0;
@@ -812,8 +825,41 @@ struct fgb_batch {
         return FGB_OK;
     }
 
+    // Rows that overflow send their particles' passes back to the 27-cell walk; when
+    // more than 1% of a step's particles overflowed (dense, compressed scenes: the
+    // ref profile's constants clump the fluid to ~200-400 neighbours within h), the
+    // capacity grows by half (at most 1024) and the solver remembers it for the
+    // bucket.  The counts arrive in st_over from steps already run.
+    int grow_rows() {
+        if (!st_over.p) return FGB_OK;
+        const uint64_t lim = std::max<uint64_t>(n / 100, 1);
+        const bool gl = list_cap && st_over.p[0] > lim && list_cap < kMaxRowCap;
+        const bool gh = hit_cap && st_over.p[1] > lim && hit_cap < kMaxRowCap;
+        if (!gl && !gh) return FGB_OK;
+        // copies queued by earlier steps would report the old capacities
+        FGB_CUDA(cudaStreamSynchronize(stream()), "grow rows sync");
+        PoolScope scope(&solver->pool);
+        const uint64_t rows = capacity ? capacity : n;
+        if (gl) {
+            list_cap = std::min<uint32_t>(kMaxRowCap, (list_cap * 3 / 2 + 3u) & ~3u);
+            FGB_CUDA(nlist.alloc(rows * list_cap), "grow neighbour lists");
+        }
+        if (gh) {
+            hit_cap = std::min<uint32_t>(kMaxRowCap, (hit_cap * 3 / 2 + 3u) & ~3u);
+            FGB_CUDA(hlist.alloc(rows * hit_cap), "grow hit lists");
+        }
+        st_over.p[0] = st_over.p[1] = 0;
+        for (auto &g : graph)
+            if (g) cudaGraphExecDestroy(g), g = nullptr;
+        graphs_ok = false;
+        solver->caps[tune_bucket(solver->params.profile, n)] = {list_cap, hit_cap};
+        return FGB_OK;
+    }
+
     int step(uint32_t steps) {
-        int rc = sync_tris();
+        int rc = grow_rows();
+        if (rc) return rc;
+        rc = sync_tris();
         if (rc) return rc;
         if (!graphs_ok) {
             rc = build_graphs();
@@ -1059,6 +1105,13 @@ static int batch_init(fgb_batch *b) {
     }
     FGB_CUDA(b->ids_dev.alloc(n), "batch alloc");
     FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
+    {
+        auto it = s->caps.find(tune_bucket(p.profile, n));
+        if (it != s->caps.end()) {
+            b->list_cap = it->second.first;
+            b->hit_cap = it->second.second;
+        }
+    }
     if (const char *e = getenv("FGB_LIST_CAP")) b->list_cap = (uint32_t)atoi(e);
     b->block = s->block;
     {
@@ -1079,6 +1132,11 @@ static int batch_init(fgb_batch *b) {
     int rc = alloc_step_arrays(b, n);
     if (rc) return rc;
     FGB_CUDA(b->err.alloc(1), "batch alloc");
+    if (b->list_cap || b->hit_cap) {
+        FGB_CUDA(b->over.alloc(2), "batch alloc");
+        FGB_CUDA(b->st_over.ensure(2), "batch alloc");
+        b->st_over.p[0] = b->st_over.p[1] = 0;
+    }
     FGB_CUDA(b->d_scenes.alloc(b->n_scenes), "batch alloc");
     FGB_CUDA(b->d_wells.alloc(std::max<size_t>(wells.size(), 1)), "batch alloc");
     FGB_CUDA(b->d_tris.alloc(1), "batch alloc");
