@@ -183,3 +183,30 @@ def test_download_into_fresh_mappings(monkeypatch):
     del out, pv
     b.close()
     solver.close()
+
+
+def test_advance_with_null_colour_and_id(monkeypatch):
+    """fgb_advance with no colour and no id arrays: both host-I/O paths give the same
+    particles, in Morton order, and leave the absent arrays alone."""
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = scenes.dam_break((18, 14, 16), (1.8, 1.6, 1.8), seed=413)
+    outs = []
+    for staged in (False, True):
+        if staged:
+            monkeypatch.setenv("FGB_HOST_IO", "staged")
+        else:
+            monkeypatch.delenv("FGB_HOST_IO", raising=False)
+        solver = SphSolver(params=params)
+        host = scenes.copy_particles(parts)
+        for _ in range(3):
+            pv = capi.particles_view(host)
+            pv.colour = None
+            pv.id = None
+            capi.check(solver.lib.fgb_advance(solver.handle, ctypes.byref(cfg), ctypes.byref(pv), None, 0, None))
+        solver.close()
+        outs.append(host)
+    monkeypatch.delenv("FGB_HOST_IO", raising=False)
+    for f in ("type", "mass", "position", "velocity"):
+        assert (outs[0][f] == outs[1][f]).all(), f
+    for f in ("id", "colour"):  # untouched
+        assert (outs[0][f] == parts[f]).all() and (outs[1][f] == parts[f]).all(), f
