@@ -50,6 +50,7 @@ __host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uin
 // Solver constants (fgb_params resolved to the values the kernels use).
 struct Phys {
     float h, hh;
+    float hh_le;      // the largest float r2 with sqrtf(r2) <= h: r2 <= hh_le is exactly sqrtf(r2) <= h
     float poly6f;     // 315 / (64 pi h^9)
     float spikyf;     // -45 / (pi h^6)
     float rho0, inv_rho0;

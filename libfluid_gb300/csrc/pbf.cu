@@ -401,6 +401,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
+            if (!(r2 <= ph.hh_le)) return;  // sqrtf(r2) > h: no contribution
             const float r = sqrtf(r2);
             if (r <= ph.h) {
                 const float t = ph.hh - r * r;
@@ -457,7 +458,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
-                const bool in = near_row ? r2 <= A.near_r2 : PROFILE == kRef ? sqrtf(r2) <= ph.h : r2 <= ph.hh;
+                const bool in = near_row ? r2 <= A.near_r2 : PROFILE == kRef ? r2 <= ph.hh_le : r2 <= ph.hh;
                 if (in) hits.add(b);
             });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
@@ -606,6 +607,7 @@ __global__ void __launch_bounds__(256)
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
+            if (!(r2 <= ph.hh_le)) return;  // sqrtf(r2) > h: no contribution
             const float r = sqrtf(r2);
             float w = 0.f;
             if (r <= ph.h) {

@@ -204,6 +204,15 @@ Phys make_phys(const fgb_params &p) {
     const float h = p.h, hh = h * h, hhh = h * h * h;
     ph.h = h;
     ph.hh = hh;
+    {
+        // sqrtf is correctly rounded and monotonic, so {r2 : sqrtf(r2) <= h} is the
+        // floats up to one threshold; the ref profile's range tests compare r2 with it
+        // and take the square root only for neighbours within h
+        float x = hh;
+        while (std::sqrt(x) > h) x = std::nextafter(x, 0.f);
+        while (std::sqrt(std::nextafter(x, INFINITY)) <= h) x = std::nextafter(x, INFINITY);
+        ph.hh_le = x;
+    }
     ph.poly6f = 315.f / (64.f * kPi * (hhh * hhh * hhh));
     ph.spikyf = -(45.f / (kPi * hhh * hhh));
     ph.rho0 = p.rho0;
