@@ -380,6 +380,33 @@ __device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const 
     for_row(A.hlist, A.hcap, a, A.hcount[a], ps, f);
 }
 
+// The step's Verlet lists on their own: each particle walks its 27 cells and keeps, in
+// walk order, every candidate within h + skin.  The first lambda pass then filters the
+// fresh lists (near rows) instead of walking, so the walk carries one row writer and
+// no kernel arithmetic.
+__global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 *__restrict__ ps) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= A.n) return;
+    if (A.type[a] == FGB_TYPE_OBSTACLE) {
+        A.ncount[a] = 0;
+        return;
+    }
+    const uint32_t key = A.keys[a];
+    const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
+    const float4 pa = ps[a];
+    RowWriter built(A.nlist, A.cap, a);
+    for_candidates(A, S, a, key, false, ps, [&](uint32_t b, const float4 &pb) {
+        const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+        if (dx * dx + dy * dy + dz * dz <= A.list_r2) built.add(b);
+    });
+    A.ncount[a] = built.close();
+    if (A.over) {  // one atomic per warp, when rows overflowed
+        const unsigned m = __activemask();
+        const unsigned lo = __ballot_sync(m, built.count > A.cap);
+        if (lo && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
+    }
+}
+
 template <int PROFILE, int MODE>
 __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
                                                 float *__restrict__ lambda, float *__restrict__ density) {
@@ -435,7 +462,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     // paths would run both one after the other
     float mcd = -1.f;
     bool done = false;
-    if (MODE != kBuild && A.near) {
+    if (MODE == kCheck && A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
             mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
@@ -453,7 +480,7 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             // phase 1: range filter (and the Verlet list on the build pass)
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
-            const bool near_row = MODE == kBuild && A.near;
+            const bool near_row = (MODE == kBuild || MODE == kFresh) && A.near;
             for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
                 const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
@@ -463,9 +490,9 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
-            if (MODE == kBuild && A.over) {  // one atomic per warp, only when rows overflowed
+            if ((MODE == kBuild || MODE == kFresh) && A.over) {  // one atomic per warp, when rows overflowed
                 const unsigned m = __activemask();
-                const unsigned lo = __ballot_sync(m, A.cap && built.count > A.cap);
+                const unsigned lo = __ballot_sync(m, MODE == kBuild && A.cap && built.count > A.cap);
                 const unsigned ho = __ballot_sync(m, A.hcap && hits.count > A.hcap);
                 if ((lo | ho) && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
                     if (lo) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
@@ -1066,7 +1093,11 @@ void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStrea
     const GatherArgs A = gather_args(s);
     const unsigned g = grid_for(s.n, s.block);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
-    if (iteration == 0) {
+    if (iteration == 0 && A.cap) {
+        k_build_lists<<<g, s.block, 0, st>>>(A, ps);
+        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+    } else if (iteration == 0) {
         if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
         else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
     } else {

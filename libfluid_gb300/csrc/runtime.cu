@@ -674,11 +674,11 @@ struct fgb_batch {
         const float4 *pin = ps_grid.p;
         for (uint32_t it = 0; it < iterations; ++it) {
             float4 *pout = ps[it & 1].p;
-            launch_lambda(s, pin, (int)it, st);
+            launch_lambda(s, pin, (int)it, st);  // the first also builds the Verlet lists (two kernels)
             mark(k, st);
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
-            l += 2;
+            l += (it == 0 && s.cap) ? 3 : 2;
             pin = pout;
         }
         if (ph.profile != FGB_PROFILE_REF) {
