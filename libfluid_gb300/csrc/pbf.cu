@@ -395,9 +395,11 @@ __global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     RowWriter built(A.nlist, A.cap, a);
+    // membership only (the passes re-test every entry exactly): a contracted r^2,
+    // within ~2e-7 of the sum of squares, against a radius rounded up by 1e-5
     for_candidates(A, S, a, key, false, ps, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-        if (dx * dx + dy * dy + dz * dz <= A.list_r2) built.add(b);
+        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
     });
     A.ncount[a] = built.close();
     if (A.over) {  // one atomic per warp, when rows overflowed
@@ -481,12 +483,14 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
             const bool near_row = (MODE == kBuild || MODE == kFresh) && A.near;
+            // membership only (the arithmetic re-tests every entry exactly): a contracted
+            // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
+            const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
             for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
                 const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-                const float r2 = dx * dx + dy * dy + dz * dz;
+                const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
                 if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
-                const bool in = near_row ? r2 <= A.near_r2 : PROFILE == kRef ? r2 <= ph.hh_le : r2 <= ph.hh;
-                if (in) hits.add(b);
+                if (r2 <= (near_row ? A.near_r2 : hit_r2)) hits.add(b);
             });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
@@ -805,10 +809,11 @@ __global__ void __launch_bounds__(256)
     } else {
         // phase 1: fluid candidates within h; phase 2: the arithmetic over them
         HitWriter hits(A, a);
+        const float hit_r2 = ph.hh * 1.000001f;  // membership only, as in the lambda filter
         for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 <= ph.hh && (!S.obstacles || __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE)) hits.add(b);
+            const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+            if (r2 <= hit_r2 && (!S.obstacles || __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE)) hits.add(b);
         });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
