@@ -703,7 +703,8 @@ __global__ void __launch_bounds__(256)
     }
     ps_out[a] = make_float4(q[0], q[1], q[2], pa.w);
     if (A.cap) {
-        // distance moved since the grid was built, for the list bound of later passes
+        // distance moved since the grid was built, for the list bound of the next pass
+        // (the per-cell maxima are cleared before every delta pass)
         const float4 g = A.ps_grid[a];
         const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);

@@ -676,6 +676,12 @@ struct fgb_batch {
             float4 *pout = ps[it & 1].p;
             launch_lambda(s, pin, (int)it, st);  // the first also builds the Verlet lists (two kernels)
             mark(k, st);
+            // the list bound at the next pass needs the neighbours' displacement at that
+            // pass only: the cell maxima restart at every delta pass (the step's first
+            // starts from the clear above), so an iteration that overshoots does not keep
+            // lists invalid after the next one has moved the particles back
+            if (it > 0 && cellmax.p)
+                FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
             l += (it == 0 && s.cap) ? 3 : 2;
