@@ -411,9 +411,10 @@ static void prefault_outputs(std::initializer_list<HostSpan> spans) {
         char *first_page = (char *)((uintptr_t)p / page * page);
         const size_t pages = (size_t)(end - first_page + page - 1) / page;
         resident.assign(pages, 0);
-        const bool known = mincore(first_page, (size_t)(end - first_page), resident.data()) == 0;
+        // a range the host does not map (mincore fails) is left to the kernel as it is
+        if (mincore(first_page, (size_t)(end - first_page), resident.data()) != 0) continue;
         for (size_t i = 0; i < pages; ++i)
-            if (!known || !(resident[i] & 1)) at.push_back(i ? first_page + i * page : p);
+            if (!(resident[i] & 1)) at.push_back(i ? first_page + i * page : p);
     }
     if (at.empty()) return;
     constexpr uint64_t kUnit = 1024;  // a pool chunk covers 16 pages
