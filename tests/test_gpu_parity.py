@@ -303,6 +303,18 @@ def test_batch_results_independent_of_composition(oracle_mod):
     solver.close()
 
 
+def test_ref_profile_parity_in_the_clumped_regime(oracle_mod):
+    """The reference's constants clump the fluid (~100-200 candidates per particle after
+    a few dozen steps): from the oracle's state after 25 steps, five more steps on a
+    fresh batch -- its rows overflow the default capacities and grow, near rows come and
+    go -- agree with the oracle step by step (keys, order and cells bit-exact)."""
+    params = capi.params(capi.PROFILE_REF, H)
+    parts, cfg = scenes.dam_break_32k()
+    for _ in range(25):
+        oracle_mod.step(params, cfg, parts)
+    _check_step(oracle_mod, params, parts, cfg, steps=5)
+
+
 def test_100_step_statistics_within_one_percent(oracle_mod):
     params = capi.params(capi.PROFILE_BASELINE, H)
     parts, cfg = scenes.dam_break_32k()
