@@ -52,3 +52,21 @@ def test_invalid_arguments_fail_without_a_gpu(lib):
     h = ctypes.c_void_p()
     assert lib.fgb_create(ctypes.byref(p), ctypes.byref(h)) == capi.FGB_ERR_INVALID
     assert lib.fgb_radix_sort_pairs_u32(None, None, None, None, 10, 8, None, 0, None) == capi.FGB_ERR_INVALID
+
+
+def test_header_constants_match_python():
+    """Every FGB_* integer #define of the header that capi.py mirrors (error codes,
+    profiles, particle types, probes, serving states, wire tags) has the same value."""
+    import os
+    import re
+    hdr = open(os.path.join(os.path.dirname(capi.__file__), "..", "include", "fluid_gb300.h")).read()
+    defines = {m.group(1): int(m.group(2), 0)
+               for m in re.finditer(r"#define\s+FGB_(\w+)\s+(0x[0-9a-fA-F]+|\d+)\b", hdr)}
+    checked = 0
+    for name, value in defines.items():
+        for py in (name, "FGB_" + name):
+            if hasattr(capi, py) and isinstance(getattr(capi, py), int):
+                assert getattr(capi, py) == value, name
+                checked += 1
+                break
+    assert checked >= 15
