@@ -599,14 +599,15 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def ncu_case():
+def ncu_case(profile="baseline"):
     """Four plain steps of dam_break_1m (per step: predict, 2 + passes sort kernels,
-    reorder, 4 x (lambda, delta), 2 vorticity kernels), then one surface of the
+    reorder, list build, 4 x (lambda, delta), 2 vorticity kernels in the baseline
+    profile; colour diffusion instead in the ref profile), then one surface of the
     256x128x128-cube lattice (position keys, sort, gather, field, scan, emit)."""
     from libfluid_gb300 import build, capi, scenes
     from libfluid_gb300.solver import Batch, SphSolver
     build.build()
-    params = capi.params(capi.PROFILE_BASELINE, 0.1)
+    params = capi.params(capi.PROFILE_REF if profile == "ref" else capi.PROFILE_BASELINE, 0.1)
     parts, cfg = scenes.dam_break_1m()
     solver = SphSolver(params=params)
     batch = Batch(solver, [(parts, cfg)])
@@ -630,9 +631,11 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default launch shapes)")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run 4 untimed steps of the workload and exit (the case that ncu captures)")
+    ap.add_argument("--ncu-profile", default="baseline", choices=["baseline", "ref"],
+                    help="physics profile of --ncu-case")
     args = ap.parse_args()
     if args.ncu_case:
-        ncu_case()
+        ncu_case(args.ncu_profile)
         return
     if args.warmup < 3:
         args.warmup = 3
