@@ -475,7 +475,13 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
         else A.near[a] = 0;
     }
     if (!done) {
-        const bool list = use_list<MODE>(A, S, a, key, mcd);
+        bool list = use_list<MODE>(A, S, a, key, mcd);
+        // ref profile, checked passes: the whole warp walks when any of its lanes must.
+        // Its clumped scenes mix lists and walks within warps, which then run both one
+        // after the other (the walk gives the same sums: the list is the walk's
+        // candidates within h + skin in walk order); the baseline profile is faster with
+        // the choice per lane.
+        if constexpr (MODE == kCheck && PROFILE == kRef) list = __all_sync(__activemask(), list);
         if (A.hcap == 0 && MODE != kBuild) {
             for_candidates(A, S, a, key, list, ps, body);
         } else {
