@@ -210,3 +210,39 @@ def test_advance_with_null_colour_and_id(monkeypatch):
         assert (outs[0][f] == outs[1][f]).all(), f
     for f in ("id", "colour"):  # untouched
         assert (outs[0][f] == parts[f]).all() and (outs[1][f] == parts[f]).all(), f
+
+
+def test_advance_with_triangles_obstacles_and_surface_matches_the_batch_path(monkeypatch):
+    """fgb_advance (on the direct path: split upload, obstacle count written into the
+    device scene table, downloads beside and inside the step) against the same frames
+    run through a batch's upload, step, surface and download, ref profile with
+    triangle colliders, obstacles and a well, colliders changing between frames."""
+    params = capi.params(capi.PROFILE_REF, H)
+    parts, cfg = scenes.dam_break((16, 14, 16), (2.0, 2.0, 2.0), seed=417)
+    parts["mass"][:] = 1.0
+    parts["type"][::13] = capi.TYPE_OBSTACLE
+    cfg.n_wells = 1
+    cfg.wells[0].centre[:] = (1.0, 1.0, 1.0)
+    cfg.wells[0].force = 2.0
+    cfg.surface = 1
+    floor = np.array([[0, 0.1, 0, 2, 0.1, 0, 0, 0.1, 2], [2, 0.1, 0, 2, 0.1, 2, 0, 0.1, 2]], np.float32)
+    ramp = np.array([[0, 0.3, 0, 2, 0.1, 0, 0, 0.3, 2]], np.float32)
+    frames = [floor, floor, ramp, None, floor]
+    solver = SphSolver(params=params)
+    host = scenes.copy_particles(parts)
+    meshes = [solver.advance(cfg, host, colliders=c) for c in frames]
+    solver.close()
+    ref_solver = SphSolver(params=params)
+    state = scenes.copy_particles(parts)
+    want = []
+    for c in frames:
+        b = _batch(monkeypatch, ref_solver, [(scenes.copy_particles(state), cfg)], staged=True)
+        b.set_colliders(0, c)
+        b.step(1)
+        want.append(b.surface(0))
+        state = b.download(0)
+        b.close()
+    ref_solver.close()
+    _same(host, state)
+    for got, ref in zip(meshes, want):  # bits: the colour columns are raw ARGB words
+        assert got.shape == ref.shape and (got.view(np.uint32) == ref.view(np.uint32)).all()
