@@ -89,7 +89,6 @@ class DevPool {
             if (it != free_.end()) {
                 void *p = it->second;
                 free_.erase(it);
-                cached_ -= c;
                 *e = cudaSuccess;
                 return p;
             }
@@ -107,23 +106,15 @@ class DevPool {
         const size_t c = size_class(bytes);
         std::lock_guard<std::mutex> lk(mu_);
         free_.emplace(c, p);
-        cached_ += c;
     }
     void trim() {
         std::lock_guard<std::mutex> lk(mu_);
         for (auto &f : free_) cudaFree(f.second);
         free_.clear();
-        cached_ = 0;
     }
-    size_t cached_bytes() {
-        std::lock_guard<std::mutex> lk(mu_);
-        return cached_;
-    }
-
   private:
     std::mutex mu_;
     std::multimap<size_t, void *> free_;
-    size_t cached_ = 0;
 };
 
 // The pool that Dev::alloc draws from on this thread (none: cudaMalloc); set by
