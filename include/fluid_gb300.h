@@ -149,6 +149,15 @@ int fgb_set_stream(fgb_solver *s, void *cuda_stream);
 int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs,
                 const fgb_triangle *colliders, size_t n_colliders, fgb_mesh *mesh_out);
 void fgb_mesh_free(fgb_mesh *m);
+/* Give every page of the host range [p, p + bytes) that is not resident a frame
+ * before kernels address it over a coherent link (what fgb_advance and the direct
+ * downloads do to the caller's arrays): a GPU store into a page the host never wrote
+ * faults to the host once per page.  keep_contents = 1 reads a byte of each such page
+ * and writes the same value back (for arrays that are also inputs: swapped-out
+ * memory, evicted file mappings); 0 stores a zero (outputs that a kernel overwrites
+ * completely).  *touched (may be NULL) receives the number of pages touched.  Host
+ * only; no counterpart in the reference, which copies through OpenCL buffers. */
+int fgb_host_ready_pages(void *p, size_t bytes, int keep_contents, uint64_t *touched);
 
 /* ---- resident scenes (a batch of one is the single-scene path) ---------- */
 /* Scenes keep particles, grid and sort scratch on the device between steps.
@@ -326,11 +335,19 @@ int fgb_radix_sort_pairs_u32(const uint32_t *d_keys_in, const uint32_t *d_vals_i
                              uint32_t *d_keys_out, uint32_t *d_vals_out, uint64_t n,
                              uint32_t key_bits, void *d_scratch, uint64_t scratch_bytes,
                              void *cuda_stream);
+/* Device error flags of the last fgb_radix_sort_pairs_u32 call that used this scratch
+ * for n keys (0: none; bit 0: a look-back wait gave up, and the output is wrong).
+ * Waits for the stream, then clears the flag. */
+int fgb_radix_sort_error(const void *d_scratch, uint64_t n, void *cuda_stream, uint32_t *flags);
 /* Single-pass exclusive prefix sum of u32 (decoupled look-back); writes the
  * total to d_total (device) when not NULL. */
 uint64_t fgb_scan_scratch_bytes(uint64_t n);
 int fgb_exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
                            void *d_scratch, uint64_t scratch_bytes, void *cuda_stream);
+/* Device error flags of the last fgb_exclusive_scan_u32 call that used this scratch
+ * for n items (0: none; bit 1: a look-back wait gave up, and the offsets are wrong).
+ * Waits for the stream, then clears the flag. */
+int fgb_scan_error(const void *d_scratch, uint64_t n, void *cuda_stream, uint32_t *flags);
 
 /* The same scan for callers that cannot allocate device memory (a host whose
  * memory manager owns every device allocation, a plugin host that forbids its
@@ -347,6 +364,21 @@ int fgb_exclusive_scan_u32(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_to
 #define FGB_SCAN_NOALLOC_MAX_N 16777216ull
 int fgb_exclusive_scan_u32_noalloc(const uint32_t *d_in, uint32_t *d_out, uint32_t *d_total, uint64_t n,
                                    void *cuda_stream);
+/* Device error flags raised by fgb_exclusive_scan_u32_noalloc calls since the last
+ * query (0: none; bit 1: a look-back wait gave up, and that call's offsets are
+ * wrong).  Waits for the stream, then clears the flag.  Allocates nothing. */
+int fgb_scan_noalloc_error(void *cuda_stream, uint32_t *flags);
+
+/* Test hook for the bounded look-back waits of the radix sort and the scans (no
+ * counterpart in the reference, which has no device-side waits).  With skip_tile !=
+ * 0xffffffff, tile skip_tile of every later sort pass and scan launch never publishes
+ * its status and every look-back wait gives up after spin_limit polls: the tile after
+ * it raises its error flag (fgb_*_error, fgb_batch_error_flags, FGB_ERR_TIMEOUT from
+ * the step calls) and returns with wrong but in-bounds output.  Nothing hangs or
+ * faults.  Step graphs keep the setting they were captured with, so a batch created
+ * while the hook is set keeps it.  fgb_test_lookback_fault(0xffffffff, 0) restores
+ * the defaults.  Process-wide; not for production use. */
+int fgb_test_lookback_fault(uint32_t skip_tile, uint32_t spin_limit);
 
 /* ---- packed record streams (the reference demo's memory-mapped result files) --
  * Replaces strucures::writeParticles / writeTriangles (samples/structures.hpp:

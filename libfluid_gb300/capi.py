@@ -250,6 +250,11 @@ _SIGS = {
     "fgb_scan_scratch_bytes": (ctypes.c_uint64, [ctypes.c_uint64]),
     "fgb_exclusive_scan_u32": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p,
                                               ctypes.c_uint64, c_void_p]),
+    "fgb_radix_sort_error": (ctypes.c_int, [c_void_p, ctypes.c_uint64, c_void_p, P(ctypes.c_uint32)]),
+    "fgb_scan_error": (ctypes.c_int, [c_void_p, ctypes.c_uint64, c_void_p, P(ctypes.c_uint32)]),
+    "fgb_scan_noalloc_error": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
+    "fgb_test_lookback_fault": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32]),
+    "fgb_host_ready_pages": (ctypes.c_int, [c_void_p, ctypes.c_size_t, ctypes.c_int, P(ctypes.c_uint64)]),
 }
 
 _lib = None

@@ -23,6 +23,16 @@ enum : uint32_t {
 // error flag and stops waiting, so a lost predecessor can never hang the GPU.
 constexpr uint32_t kSpinLimit = 1u << 22;
 
+// Look-back settings of one sort pass or scan launch, passed by value.  Normally
+// skip_tile is ~0u and spin_limit kSpinLimit.  fgb_test_lookback_fault sets a tile
+// that never publishes its status and a small spin limit, so that the tile after it
+// runs out of polls, raises its error flag and returns: the tested form of a lost
+// predecessor.
+struct LookbackCtl {
+    uint32_t skip_tile;
+    uint32_t spin_limit;
+};
+
 constexpr float kKernelEpsilon = 0.00000001f;  // oclsph_kernel.h:24
 constexpr float kPiF = 3.14159265358979323846f;
 

@@ -24,6 +24,10 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
                              uint32_t *vals_out, uint64_t n, uint32_t key_bits, void *scratch,
                              uint64_t scratch_bytes, cudaStream_t stream, uint32_t *err, uint64_t *launches);
 
+// Copy a device error-flag word to *flags and clear it, after the work queued on
+// stream (synchronises the stream; allocates nothing).
+int read_clear_flag(void *d_flag, cudaStream_t stream, uint32_t *flags, const char *where);
+
 // prefix scan of a u32 array (scan.cu)
 uint64_t scan_u32_scratch_bytes(uint64_t n);
 cudaError_t scan_u32(const uint32_t *in, uint32_t *out, uint32_t *total, uint64_t n, void *scratch,

@@ -379,20 +379,24 @@ static void parallel_for(uint64_t n, F &&f) {
     HostPool::get().run(n, f);
 }
 
-// Give the pages of the caller's output arrays a frame on the host before a kernel
-// writes them over the coherent link.  A GPU store to a page that the host never
-// wrote (fresh calloc or mmap memory) faults to the host once per page -- ~17 ms
-// for a 1M-particle download into fresh arrays -- whereas one host store per page
-// costs ~2 us on a fresh page.  mincore() finds the pages that are not resident
-// (for reused arrays: none, at the cost of one system call per array); each gets a
-// store of 0 into a byte that the kernel then overwrites (every element of every
-// array passed is written).  A load first would cost a second fault (zero page,
-// then copy-on-write).
+// Give the pages of the caller's arrays a frame on the host before a kernel writes
+// them over the coherent link.  A GPU store to a page that the host never wrote
+// (fresh calloc or mmap memory) faults to the host once per page -- ~17 ms for a
+// 1M-particle download into fresh arrays -- whereas one host store per page costs
+// ~2 us on a fresh page.  mincore() finds the pages that are not resident (for
+// reused arrays: none, at the cost of one system call per array).  For arrays that
+// are only outputs, each such page gets a store of 0 into a byte that the kernel then
+// overwrites (every element of every array passed is written); a load first would
+// cost a second fault (zero page, then copy-on-write).  For arrays that are also
+// inputs (fgb_advance works in place), a page that is not resident can still hold
+// data -- swapped-out memory, or a file mapping whose page was evicted -- so each
+// gets a load of a byte and a store of the same value back: the page is read in
+// and made writable without changing what the kernels will read.
 struct HostSpan {
     void *p;
     size_t bytes;
 };
-static void prefault_outputs(std::initializer_list<HostSpan> spans) {
+static int ready_pages(std::initializer_list<HostSpan> spans, bool keep_contents) {
     static const size_t page = (size_t)sysconf(_SC_PAGESIZE) > 0 ? (size_t)sysconf(_SC_PAGESIZE) : 4096;
     std::vector<char *> at;
     std::vector<unsigned char> resident;
@@ -407,12 +411,17 @@ static void prefault_outputs(std::initializer_list<HostSpan> spans) {
         for (size_t i = 0; i < pages; ++i)
             if (!(resident[i] & 1)) at.push_back(i ? first_page + i * page : p);
     }
-    if (at.empty()) return;
+    if (at.empty()) return 0;
     constexpr uint64_t kUnit = 1024;  // a pool chunk covers 16 pages
     parallel_for(at.size() * kUnit, [&](uint64_t lo, uint64_t hi) {
-        for (uint64_t i = (lo + kUnit - 1) / kUnit; i * kUnit < hi; ++i) *(volatile char *)at[i] = 0;
+        for (uint64_t i = (lo + kUnit - 1) / kUnit; i * kUnit < hi; ++i) {
+            volatile char *q = at[i];
+            *q = keep_contents ? *q : (char)0;
+        }
     });
+    return (int)std::min<size_t>(at.size(), 0x7fffffff);
 }
+static void prefault_outputs(std::initializer_list<HostSpan> spans) { ready_pages(spans, false); }
 
 // Pieces of the pipelined upload and download: host packing or unpacking of one
 // piece overlaps the copies of the others.
@@ -492,6 +501,9 @@ struct fgb_batch {
     // the step; grow_rows() enlarges the capacities when more than 1% did
     Dev<uint32_t> over;
     Pinned<uint32_t> st_over;
+    // the device error flags (err) as of the end of each step, copied by the step
+    // graph; fgb_batch_step, fgb_batch_sync and fgb_advance turn them into a status
+    Pinned<uint32_t> st_flags;
     Dev<char> wire;         // packed-record staging (wire.cu)
     int cur = 0;
     // step
@@ -687,6 +699,7 @@ struct fgb_batch {
         if (over.p)
             FGB_CUDA(cudaMemcpyAsync(st_over.p, over.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
                      "step: overflow counters");
+        FGB_CUDA(cudaMemcpyAsync(st_flags.p, err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "step: error flags");
         FGB_CUDA(cudaGetLastError(), "step: launch");
         launches_per_step = l;
         if (timing) n_stages = k ? k - 1 : 0;
@@ -990,6 +1003,32 @@ static int mesh_assign(fgb_mesh *m, const fgb_mesh_triangle *dev, uint64_t count
     return FGB_OK;
 }
 
+// Status of a batch's device error flags: FGB_OK when none is set, else the status
+// code of the most serious flag with a message naming them all.
+static int flags_status(uint32_t f, const char *where) {
+    if (!f) return FGB_OK;
+    char msg[256];
+    snprintf(msg, sizeof msg,
+             "%s: device error flags 0x%x (%s%s%s%s%s); fgb_batch_error_flags reads and clears them", where, f,
+             f & ERR_SORT_LOOKBACK ? "sort look-back wait gave up " : "",
+             f & ERR_SCAN_LOOKBACK ? "scan look-back wait gave up " : "",
+             f & ERR_CELL_RANGE ? "key outside its cell table " : "",
+             f & ERR_MESH_CAPACITY ? "more triangles than the buffer holds " : "",
+             f & ERR_WELD_TABLE ? "welding table full " : "");
+    if (f & (ERR_SORT_LOOKBACK | ERR_SCAN_LOOKBACK)) return fail(FGB_ERR_TIMEOUT, msg);
+    if (f & (ERR_MESH_CAPACITY | ERR_WELD_TABLE)) return fail(FGB_ERR_CAPACITY, msg);
+    return fail(FGB_ERR_INVALID, msg);
+}
+
+// Device error flags as of now (synchronises the batch's stream).
+static int batch_flags_now(fgb_batch *b, uint32_t *f) {
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemcpyAsync(b->st_flags.p, b->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "error flags");
+    FGB_CUDA(cudaStreamSynchronize(st), "error flags");
+    *f = b->st_flags.p[0];
+    return FGB_OK;
+}
+
 // The per-particle arrays a step rebuilds (sort keys, p*, lists, lambda, ...), for
 // `cap` particles; their contents do not outlive a step.
 static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
@@ -1139,6 +1178,8 @@ static int batch_init(fgb_batch *b) {
     int rc = alloc_step_arrays(b, n);
     if (rc) return rc;
     FGB_CUDA(b->err.alloc(1), "batch alloc");
+    FGB_CUDA(b->st_flags.ensure(1), "batch alloc");
+    b->st_flags.p[0] = 0;
     if (b->list_cap || b->hit_cap) {
         FGB_CUDA(b->over.alloc(2), "batch alloc");
         FGB_CUDA(b->st_over.ensure(2), "batch alloc");
@@ -1646,6 +1687,10 @@ int fgb_batch_set_colliders(fgb_batch *b, uint32_t scene, const fgb_triangle *tr
 int fgb_batch_step(fgb_batch *b, uint32_t steps) {
     if (!b) return fail(FGB_ERR_INVALID, "step: null batch");
     if (b->n == 0) return FGB_OK;
+    // flags raised by steps that have finished (copied by their graphs): the state is
+    // suspect, so nothing more is queued until fgb_batch_error_flags clears them
+    int rc = flags_status(b->st_flags.p[0], "step");
+    if (rc) return rc;
     return b->step(steps);
 }
 
@@ -1665,7 +1710,10 @@ int fgb_batch_surface(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out) {
     if (rc) return rc;
     rc = b->surface_emit(t);
     if (rc) return rc;
-    return mesh_assign(mesh_out, b->tris_out.p, t, b->stream());
+    rc = mesh_assign(mesh_out, b->tris_out.p, t, b->stream());
+    uint32_t f = 0;
+    if (!rc) rc = batch_flags_now(b, &f);
+    return rc ? rc : flags_status(f, "surface");
 }
 
 int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts) {
@@ -1688,6 +1736,10 @@ int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts) {
             firsts[k] = (uint32_t)t;
     }
     FGB_CUDA(cudaStreamSynchronize(st), "surface_all: sync");
+    uint32_t f = 0;
+    rc = batch_flags_now(b, &f);
+    if (!rc) rc = flags_status(f, "surface_all");
+    if (rc) return rc;
     for (uint32_t k = 0; k < b->n_scenes; ++k) b->surf_tri_first[k] = firsts[k];
     b->surf_tri_first[b->n_scenes] = t;
     for (uint32_t k = 0; k < b->n_scenes; ++k)
@@ -1738,7 +1790,7 @@ int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out) {
 int fgb_batch_sync(fgb_batch *b) {
     if (!b) return fail(FGB_ERR_INVALID, "sync: null batch");
     FGB_CUDA(cudaStreamSynchronize(b->stream()), "sync");
-    return FGB_OK;
+    return flags_status(b->st_flags.p[0], "sync");  // as of the last step's end
 }
 
 int fgb_batch_prepare(fgb_batch *b) {
@@ -1758,6 +1810,7 @@ int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
     FGB_CUDA(cudaMemcpyAsync(flags, b->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "error_flags");
     FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), st), "error_flags");
     FGB_CUDA(cudaStreamSynchronize(st), "error_flags");
+    b->st_flags.p[0] = 0;
     return FGB_OK;
 }
 
@@ -2035,6 +2088,9 @@ int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out) {
 //                positions and velocities into the caller's arrays -> [surface]
 //   io_stream:   colours, ids, slots in (the step's reorder waits for them) ->
 //                after the grid is built: types, colours, ids, masses out
+// The frame's device error flags (raised by its step) as its status.
+static int advance_flags(fgb_batch *b) { return flags_status(b->st_flags.p[0], "advance"); }
+
 static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs, fgb_mesh *mesh_out) {
     const uint64_t n = xs->n;
     if (!xs->position || !xs->velocity || !xs->mass || !xs->type)
@@ -2045,6 +2101,11 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
     const int c = b->cur, next = c ^ 1;
     uint32_t *obstacles = &b->d_scenes.p[0].obstacles;
     const HostParticlesIn in{xs->position, xs->velocity, xs->mass, xs->type, xs->colour, xs->id};
+    // the arrays are inputs and outputs: their pages are readied, contents kept, before
+    // any kernel of the frame reads or stores into them
+    ready_pages({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
+                 {xs->colour, 4 * n}, {xs->id, 8 * n}},
+                true);
     FGB_CUDA(cudaMemsetAsync(obstacles, 0, sizeof(uint32_t), st), "advance: upload");
     launch_pack_motion(in, n, b->x[c].p, b->v[c].p, b->type[c].p, obstacles, st);
     FGB_CUDA(cudaGetLastError(), "advance: upload kernel");
@@ -2058,9 +2119,6 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
     launch_fill_u32(b->keys_sorted.p, n, 0u, st);  // scene 0's key prefix for the prediction
     b->ids[0].clear();
     b->ids_stale[0] = 0;
-    // output pages readied before any kernel of the frame stores into them
-    prefault_outputs({{xs->position, 12 * n}, {xs->velocity, 12 * n}, {xs->mass, 4 * n}, {xs->type, 4 * n},
-                      {xs->colour, 4 * n}, {xs->id, 8 * n}});
     // the step's last kernel stores positions and velocities into the caller's arrays
     b->st_hout.p[0] = HostParticlesOut{xs->position, xs->velocity, nullptr, nullptr, nullptr, nullptr};
     FGB_CUDA(cudaMemcpyAsync(b->hout_dev.p, b->st_hout.p, sizeof(HostParticlesOut), cudaMemcpyHostToDevice, st),
@@ -2082,7 +2140,7 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
     FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
     FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
     b->h_scenes[0].obstacles = b->st_count.p[0];  // the device table has it already
-    return FGB_OK;
+    return advance_flags(b);
 }
 
 int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const fgb_triangle *colliders,
@@ -2116,6 +2174,10 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     fgb_batch *b = s->cached;
     int rc = fgb_batch_set_colliders(b, 0, colliders, n_colliders);
     if (rc) return rc;
+    // a frame's flags are its own: the particles are uploaded afresh every frame (the
+    // previous frame has finished, so the pinned copy is not being written)
+    b->st_flags.p[0] = 0;
+    FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), b->stream()), "advance: error flags");
     if (b->advance_io && b->io_stream) return advance_direct(b, cfg, xs, mesh_out);
     rc = batch_upload(b, 0, xs);
     if (rc) return rc;
@@ -2125,7 +2187,15 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
         rc = fgb_batch_surface(b, 0, mesh_out);
         if (rc) return rc;
     }
-    return batch_download(b, 0, xs);
+    rc = batch_download(b, 0, xs);
+    return rc ? rc : advance_flags(b);
+}
+
+int fgb_host_ready_pages(void *p, size_t bytes, int keep_contents, uint64_t *touched) {
+    if (bytes && !p) return fail(FGB_ERR_INVALID, "ready_pages: null pointer");
+    const int t = ready_pages({{p, bytes}}, keep_contents != 0);
+    if (touched) *touched = (uint64_t)t;
+    return FGB_OK;
 }
 
 void fgb_mesh_free(fgb_mesh *m) {

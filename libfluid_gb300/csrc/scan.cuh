@@ -16,6 +16,9 @@
 
 namespace fgb {
 
+// Look-back settings of the next launches (sort.cu; fgb_test_lookback_fault).
+LookbackCtl lookback_ctl();
+
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -26,7 +29,7 @@ constexpr unsigned long long kScanInclusive = 2ull << 32;
 template <class Load>
 __global__ void __launch_bounds__(kScanThreads)
     k_scan(Load load, uint32_t *__restrict__ out, uint64_t n, unsigned long long *status,
-           uint32_t *tile_counter, uint32_t *total, uint32_t *err) {
+           uint32_t *tile_counter, uint32_t *total, uint32_t *err, LookbackCtl ctl) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_warp[kScanThreads / 32];
     __shared__ uint32_t s_prefix;
@@ -61,17 +64,21 @@ __global__ void __launch_bounds__(kScanThreads)
     }
     if (tid == 0) {
         unsigned long long *my = status + tile;
+        // a skipped tile (fgb_test_lookback_fault only) publishes nothing
+        const bool publish = tile != ctl.skip_tile;
         uint32_t prefix = 0;
         if (tile == 0) {
-            st_relaxed64(my, kScanInclusive | block_total);
+            if (publish) st_relaxed64(my, kScanInclusive | block_total);
         } else {
-            st_relaxed64(my, kScanAggregate | block_total);
+            if (publish) st_relaxed64(my, kScanAggregate | block_total);
             int t = (int)tile - 1;
             uint32_t spins = 0;
             while (t >= 0) {
                 unsigned long long s = ld_relaxed64(status + t);
                 if ((s >> 32) == 0) {
-                    if (++spins > kSpinLimit) {
+                    // the wait gives up with a partial prefix; outputs are then wrong
+                    // but every store stays at its own index below n
+                    if (++spins > ctl.spin_limit) {
                         raise_error(err, ERR_SCAN_LOOKBACK);
                         break;
                     }
@@ -81,7 +88,7 @@ __global__ void __launch_bounds__(kScanThreads)
                 if (s & kScanInclusive) break;
                 --t;
             }
-            st_relaxed64(my, kScanInclusive | (unsigned long long)(uint32_t)(prefix + block_total));
+            if (publish) st_relaxed64(my, kScanInclusive | (unsigned long long)(uint32_t)(prefix + block_total));
         }
         s_prefix = prefix;
         uint64_t tiles = (n + kScanTile - 1) / kScanTile;
@@ -117,7 +124,8 @@ cudaError_t scan_launch(Load load, uint32_t *out, uint32_t *total, uint64_t n, v
     uint32_t *counter = (uint32_t *)((char *)scratch + tiles * sizeof(unsigned long long));
     cudaError_t e = cudaMemsetAsync(scratch, 0, tiles * sizeof(unsigned long long) + sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
-    k_scan<Load><<<(unsigned)tiles, kScanThreads, 0, stream>>>(load, out, n, status, counter, total, err);
+    k_scan<Load><<<(unsigned)tiles, kScanThreads, 0, stream>>>(load, out, n, status, counter, total, err,
+                                                               lookback_ctl());
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

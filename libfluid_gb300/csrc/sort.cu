@@ -10,6 +10,7 @@
 // publishes its per-digit counts, looks back over earlier tiles' published counts
 // (decoupled look-back) to find where its keys start, and scatters.  A pre-pass
 // histograms all digits of all passes at once.  Every look-back wait is bounded.
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -68,7 +69,8 @@ __global__ void __launch_bounds__(256) k_radix_offsets(const uint32_t *__restric
 __global__ void __launch_bounds__(kSortThreads) k_onesweep(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, uint32_t n, int shift,
-    const uint32_t *__restrict__ offsets, uint32_t *status, uint32_t *tile_counter, uint32_t *err) {
+    const uint32_t *__restrict__ offsets, uint32_t *status, uint32_t *tile_counter, uint32_t *err,
+    LookbackCtl ctl) {
     __shared__ uint32_t s_tile;
     __shared__ uint32_t s_hist[kSortWarps][kRadix + 1];
     __shared__ uint32_t s_base[kRadix + 1];
@@ -113,17 +115,21 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
             run += c;
         }
         uint32_t *my = status + (size_t)tile * kRadix + d;
+        // a skipped tile (fgb_test_lookback_fault only) publishes nothing
+        const bool publish = tile != ctl.skip_tile;
         uint32_t excl = 0;
         if (tile == 0) {
-            st_relaxed(my, kFlagInclusive | run);
+            if (publish) st_relaxed(my, kFlagInclusive | run);
         } else {
-            st_relaxed(my, kFlagAggregate | run);
+            if (publish) st_relaxed(my, kFlagAggregate | run);
             int t = (int)tile - 1;
             uint32_t spins = 0;
             while (t >= 0) {
                 uint32_t s = ld_relaxed(status + (size_t)t * kRadix + d);
                 if ((s & ~kValueMask) == 0) {
-                    if (++spins > kSpinLimit) {
+                    // a timed-out wait keeps the partial prefix: a sum over a subset of
+                    // the earlier tiles' counts, so every scatter index stays below n
+                    if (++spins > ctl.spin_limit) {
                         raise_error(err, ERR_SORT_LOOKBACK);
                         break;
                     }
@@ -133,7 +139,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(
                 if (s & kFlagInclusive) break;
                 --t;
             }
-            st_relaxed(my, kFlagInclusive | (excl + run));
+            if (publish) st_relaxed(my, kFlagInclusive | (excl + run));
         }
         s_base[d] = offsets[d] + excl;
     }
@@ -184,6 +190,15 @@ SortLayout sort_layout(uint64_t n) {
 
 }  // namespace
 
+namespace {
+std::atomic<uint64_t> g_lookback{(uint64_t)kSpinLimit << 32 | 0xffffffffull};
+}  // namespace
+
+LookbackCtl lookback_ctl() {
+    const uint64_t v = g_lookback.load(std::memory_order_relaxed);
+    return LookbackCtl{(uint32_t)v, (uint32_t)(v >> 32)};
+}
+
 uint64_t radix_scratch_bytes(uint64_t n) { return sort_layout(n).total; }
 
 int radix_passes(uint32_t key_bits) {
@@ -207,6 +222,7 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
     uint32_t *alt_k = (uint32_t *)(s + L.alt_keys);
     uint32_t *alt_v = (uint32_t *)(s + L.alt_vals);
     const int passes = radix_passes(key_bits);
+    const LookbackCtl ctl = lookback_ctl();
     // hist, offsets, counters and the status words of every pass start at zero
     cudaError_t e = cudaMemsetAsync(s, 0, L.alt_keys, stream);
     if (e != cudaSuccess) return e;
@@ -221,7 +237,7 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
         uint32_t *dv = to_out ? vals_out : alt_v;
         k_onesweep<<<L.tiles, kSortThreads, 0, stream>>>(
             src_k, src_v, dk, dv, (uint32_t)n, p * kRadixBits, offsets + p * kRadix,
-            status + (size_t)p * L.tiles * kRadix, counters + p, err);
+            status + (size_t)p * L.tiles * kRadix, counters + p, err, ctl);
         src_k = dk;
         src_v = dv;
     }
@@ -254,6 +270,20 @@ int fgb_radix_sort_pairs_u32(const uint32_t *d_keys_in, const uint32_t *d_vals_i
         e = fgb::radix_sort_pairs(d_keys_in, d_vals_in, d_keys_out, d_vals_out, n, key_bits, d_scratch, core, st,
                                   err, nullptr);
     if (e != cudaSuccess) return fgb::fail_cuda(e, "radix sort");
+    return FGB_OK;
+}
+
+int fgb_radix_sort_error(const void *d_scratch, uint64_t n, void *cuda_stream, uint32_t *flags) {
+    if (!d_scratch || !flags) return fgb::fail(FGB_ERR_INVALID, "radix sort error: null argument");
+    return fgb::read_clear_flag((char *)d_scratch + fgb::radix_scratch_bytes(n), (cudaStream_t)cuda_stream, flags,
+                                "radix sort error");
+}
+
+int fgb_test_lookback_fault(uint32_t skip_tile, uint32_t spin_limit) {
+    if (skip_tile != 0xffffffffu && spin_limit == 0)
+        return fgb::fail(FGB_ERR_INVALID, "lookback fault: a skipped tile needs a spin limit above 0");
+    if (skip_tile == 0xffffffffu) spin_limit = fgb::kSpinLimit;
+    fgb::g_lookback.store((uint64_t)spin_limit << 32 | skip_tile, std::memory_order_relaxed);
     return FGB_OK;
 }
 }
