@@ -3,8 +3,8 @@
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
  * library; the product never does.  See pbf_oracle.h for the parity status
- * (integer parts pinned against the reference's own headers; float parts a
- * restatement, unpinned against the unbuildable reference PBF).
+ * (integer parts pinned against the reference's own headers; float parts pinned
+ * against the reference's own kernel bodies compiled as C++, ref_kernels.cpp).
  *
  * The algorithm follows tom91136/libfluid:
  *   predict ............ include/fluid/oclsph.hpp:289-325 (advectAndCopy)
@@ -690,6 +690,7 @@ int orc_step(const fgb_params *p, const fgb_config *c, size_t n, uint64_t *id, i
     PERMUTE(float, ps, 3);
     PERMUTE(uint32_t, key, 1);
 
+    if (probe && probe->pstar) memcpy(probe->pstar, ps, 3 * n * sizeof(float));
     uint32_t *cells = (uint32_t *)malloc((size_t)s.g.table_n * 2 * sizeof(uint32_t));
     build_cells(n, key, s.g.table_n, cells);
     uint32_t *cxyz = (uint32_t *)malloc(3 * n * sizeof(uint32_t));

@@ -9,11 +9,14 @@
  *   - Morton keys and the marching-cubes tables are PINNED: tests compare them with
  *     the reference's own curves.h / mctable.hpp / mc.h compiled from the reference
  *     tree (oracle/ref_shim.cpp) and with committed golden vectors (tests/golden).
- *   - The floating-point PBF and MC arithmetic is a restatement of the cited
- *     reference lines; the reference's PBF cannot be built here (its OpenCL path
- *     needs OpenCL headers, its OpenMP path needs GLM and does not compile), so
- *     float parity with the reference itself is UNPINNED.  Formula-level known
- *     answers (tests/test_oracle_known_answers.py) pin the kernels to mathematics.
+ *   - The floating-point PBF and MC arithmetic of the ref profile is PINNED to the
+ *     reference's own OpenCL kernel bodies (sph_diffuse, sph_lambda, sph_delta with
+ *     the triangle collider, sph_finalise, mc_lattice, mc_size, mc_eval) compiled as
+ *     C++ (oracle/ref_kernels.cpp): tests/test_oracle_ref_kernels.py compares them
+ *     on the same predicted state at the stated tolerances, live and against
+ *     committed vectors (tests/golden/reference_kernels.npz).  Not pinned by
+ *     reference code: the host-side prediction (GLM host code) and the baseline
+ *     profile's XSPH, vorticity and density field, which have no reference code.
  */
 #ifndef PBF_ORACLE_H
 #define PBF_ORACLE_H
@@ -45,6 +48,7 @@ typedef struct orc_probe {
     uint32_t *cells;    /* 2 * table_n, {start, end} per key (0,0 when empty) */
     float *lambda;      /* n, last iteration */
     float *density;     /* n, last iteration */
+    float *pstar;       /* 3n, predicted p* in sorted order, before the solver iterations */
 } orc_probe;
 
 uint32_t orc_morton(uint32_t x, uint32_t y, uint32_t z);
