@@ -160,84 +160,164 @@ def cpu_sample(seconds, params, make_scene):
                       f"{dt:.1f} s"}
 
 
-def bench_batched(params, steps=20, mc_every=10, tune=True):
-    """Workload 4: 64 mixed scenes in one batch vs the same scenes stepped one by one."""
+# Algorithmic bytes of marching cubes: per lattice sample its value, normal and colour
+# written (20); per cube its case byte, triangle count and offset (~21, the 8 corner
+# values re-read from cache); per triangle its 84-byte record written.
+MC_BYTES = {"sample": 20, "cube": 21, "triangle": 84}
+
+
+def time_surface(batch, stream, k=0):
+    """Marching cubes of scene k's current state (position grid, field, case scan,
+    emit; triangles left on the device), timed with CUDA events on the solver's
+    stream, with the algorithmic bytes of the lattice over that time."""
     import torch
-    from libfluid_gb300 import scenes
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batch.sync()
+    e0.record(stream)
+    counts = batch.surface_all()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    gi = batch.grid_info(k)
+    samples = int(gi.lattice[0]) * int(gi.lattice[1]) * int(gi.lattice[2])
+    cubes = (int(gi.lattice[0]) - 1) * (int(gi.lattice[1]) - 1) * (int(gi.lattice[2]) - 1)
+    tris = int(counts[k])
+    algo = MC_BYTES["sample"] * samples + MC_BYTES["cube"] * cubes + MC_BYTES["triangle"] * tris
+    peak, peak_kind = measured_peaks()
+    gbs = algo / (ms * 1e-3) / 1e9
+    return {"cells": [int(gi.lattice[0]) - 1, int(gi.lattice[1]) - 1, int(gi.lattice[2]) - 1], "samples": samples,
+            "triangles": tris, "ms": ms, "algorithmic_bytes": algo, "achieved_gbs": gbs, "hbm_frac": gbs / peak,
+            "peak_kind": peak_kind, "error_flags": batch.error_flags()}
+
+
+def dropin_frames(parts, cfg, warmup, frames):
+    """The drop-in as a libfluid application calls it: tests/cpp/dropin_frames.cpp
+    drives cuda::SphSolver::advance on a std::vector<fluid::Particle> (read and written
+    in place by the library) for `warmup` + `frames` frames; returns its JSON line."""
+    from libfluid_gb300 import build, capi
+    lib_dir = os.path.dirname(build.build())
+    exe = os.path.join(lib_dir, "dropin_frames")
+    src = os.path.join(ROOT, "tests", "cpp", "dropin_frames.cpp")
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src), os.path.getmtime(build.LIB)):
+        cmd = ["g++", "-std=c++14", "-O2", "-I" + os.path.join(ROOT, "include"), src, "-L" + lib_dir, "-lfluidgb",
+               "-Wl,-rpath," + lib_dir, "-o", exe]
+        subprocess.run(cmd, check=True, capture_output=True)
+    import numpy as np
+    rec = capi.to_records(parts)
+    fd, path = tempfile.mkstemp(suffix=".scene")
+    with os.fdopen(fd, "wb") as f:
+        f.write(np.uint64(len(rec)).tobytes())
+        f.write(rec.tobytes())
+        f.write(np.array([cfg.dt, cfg.scale, 0.0, cfg.isolevel], np.float32).tobytes())
+        f.write(np.uint32(cfg.iterations).tobytes())
+        sphere = list(cfg.sphere) if cfg.sphere_enabled else [0.0, 0.0, 0.0, 0.0]
+        f.write(np.array([*cfg.constant_force, *cfg.min_bound, *cfg.max_bound, *sphere], np.float32).tobytes())
+    try:
+        r = subprocess.run([exe, path, str(warmup), str(frames), "1"], capture_output=True, text=True, timeout=600)
+    finally:
+        os.unlink(path)
+    if r.returncode != 0:
+        return {"error": (r.stderr or "")[-300:], "rc": r.returncode}
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def bench_batched(params, steps=100, mc_every=10, tune=True, rank=0, world=1):
+    """Workload 4: 64 mixed scenes in one batch vs the same scenes stepped one by one,
+    `steps` steps with every scene's surface each `mc_every`.  With several ranks
+    each steps its share of the scenes (partition.local_scenes, no collective on the
+    data path); an arm's time is its slowest rank's."""
+    import torch
+    from libfluid_gb300 import partition, scenes
     from libfluid_gb300.solver import Batch, SphSolver
     specs = scenes.batched_64()
-    total = sum(len(p["mass"]) for p, _ in specs)
-    solver = SphSolver(params=params)
-    if tune:
-        # both arms tuned on copies: the batch's bucket, and one scene per single's bucket
-        t = Batch(solver, [(scenes.copy_particles(p), c) for p, c in specs])
-        t.autotune(3)
-        t.close()
-        seen = set()
-        for p, c in specs:
-            bucket = len(p["mass"]).bit_length()
-            if bucket in seen:
-                continue
-            seen.add(bucket)
-            t = Batch(solver, [(scenes.copy_particles(p), c)])
+
+    def run_local(mine):
+        local = [spec for _, spec in mine]
+        total = sum(len(p["mass"]) for p, _ in local)
+        solver = SphSolver(params=params)
+        if tune:
+            # both arms tuned on copies: the batch's bucket, and one scene per single's bucket
+            t = Batch(solver, [(scenes.copy_particles(p), c) for p, c in local])
             t.autotune(3)
             t.close()
-    batch = Batch(solver, [(scenes.copy_particles(p), c) for p, c in specs])
-    batch.step(3)
-    batch.sync()
-    launches0 = batch.launches
-    t0 = time.perf_counter()
-    tris = 0
-    for s in range(1, steps + 1):
-        batch.step(1)
-        if s % mc_every == 0:
-            tris += sum(batch.surface_all())
-    batch.sync()
-    t_batched = time.perf_counter() - t0
-    launches = batch.launches - launches0
-    batch.close()
-    singles = [Batch(solver, [(scenes.copy_particles(p), c)]) for p, c in specs]
-    for b in singles:
-        b.step(3)
-    for b in singles:
-        b.sync()
-    t0 = time.perf_counter()
-    for s in range(1, steps + 1):
+            seen = set()
+            for p, c in local:
+                bucket = len(p["mass"]).bit_length()
+                if bucket in seen:
+                    continue
+                seen.add(bucket)
+                t = Batch(solver, [(scenes.copy_particles(p), c)])
+                t.autotune(3)
+                t.close()
+        batch = Batch(solver, [(scenes.copy_particles(p), c) for p, c in local])
+        batch.step(3)
+        batch.sync()
+        launches0 = batch.launches
+        partition.barrier()
+        t0 = time.perf_counter()
+        tris = 0
+        for s in range(1, steps + 1):
+            batch.step(1)
+            if s % mc_every == 0:
+                tris += sum(batch.surface_all())
+        batch.sync()
+        t_batched = time.perf_counter() - t0
+        launches = batch.launches - launches0
+        halo = batch.halo_usage()
+        batch.close()
+        singles = [Batch(solver, [(scenes.copy_particles(p), c)]) for p, c in local]
         for b in singles:
-            b.step(1)
-        if s % mc_every == 0:
+            b.step(3)
+        for b in singles:
+            b.sync()
+        partition.barrier()
+        t0 = time.perf_counter()
+        for s in range(1, steps + 1):
             for b in singles:
-                b.surface(0)
-    for b in singles:
-        b.sync()
-    t_loop = time.perf_counter() - t0
-    for b in singles:
-        b.close()
-    solver.close()
-    # the plain single-scene step as a libfluid user calls it: one drop-in solver per
-    # scene, advance() per frame with host arrays, a surface every mc_every frames
-    plain = [(SphSolver(params=params), scenes.copy_particles(p), c) for p, c in specs]
-    for sv, p, c in plain:
-        for _ in range(3):
-            sv.advance(c, p)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in range(1, steps + 1):
+                b.step(1)
+            if s % mc_every == 0:
+                for b in singles:
+                    b.surface(0)
+        for b in singles:
+            b.sync()
+        t_loop = time.perf_counter() - t0
+        for b in singles:
+            b.close()
+        solver.close()
+        # the plain single-scene step as a libfluid user calls it: one drop-in solver
+        # per scene, advance() per frame with host arrays, a surface every mc_every frames
+        plain = [(SphSolver(params=params), scenes.copy_particles(p), c) for p, c in local]
         for sv, p, c in plain:
-            c.surface = 1 if s % mc_every == 0 else 0
-            sv.advance(c, p)
-            c.surface = 0
-    t_plain = time.perf_counter() - t0
-    for sv, _, _ in plain:
-        sv.close()
-    torch.cuda.synchronize()
-    v_b = total * steps / t_batched
-    v_l = total * steps / t_loop
-    v_p = total * steps / t_plain
+            for _ in range(3):
+                sv.advance(c, p)
+        torch.cuda.synchronize()
+        partition.barrier()
+        t0 = time.perf_counter()
+        for s in range(1, steps + 1):
+            for sv, p, c in plain:
+                c.surface = 1 if s % mc_every == 0 else 0
+                sv.advance(c, p)
+                c.surface = 0
+        t_plain = time.perf_counter() - t0
+        for sv, _, _ in plain:
+            sv.close()
+        torch.cuda.synchronize()
+        return {"particles": total, "batched_s": t_batched, "loop_s": t_loop, "plain_s": t_plain,
+                "launches": launches, "triangles": tris, "halo_ctas": halo[1], "ctas": halo[0]}
+
+    per_rank = partition.sharded_run(specs, rank, world, run_local)
+    r = partition.combine(per_rank, sum_keys=("particles", "launches", "triangles", "halo_ctas", "ctas"),
+                          max_keys=("batched_s", "loop_s", "plain_s"))
+    total = r["particles"]
+    v_b = total * steps / r["batched_s"]
+    v_l = total * steps / r["loop_s"]
+    v_p = total * steps / r["plain_s"]
     return {"workload": "batched_64", "scenes": len(specs), "particles": total, "steps": steps,
-            "surface_every": mc_every, "batched_particle_steps_per_s": v_b, "per_scene_loop_particle_steps_per_s": v_l,
-            "speedup": v_b / v_l, "per_scene_advance_loop_particle_steps_per_s": v_p,
-            "speedup_vs_advance_loop": v_b / v_p, "batched_launches": launches, "triangles": tris,
+            "surface_every": mc_every, "ranks": world, "batched_particle_steps_per_s": v_b,
+            "per_scene_loop_particle_steps_per_s": v_l, "speedup": v_b / v_l,
+            "per_scene_advance_loop_particle_steps_per_s": v_p, "speedup_vs_advance_loop": v_b / v_p,
+            "batched_launches": r["launches"], "triangles": r["triangles"],
+            "halo_ctas_fraction": r["halo_ctas"] / r["ctas"] if r["ctas"] else 0.0,
             "arms": "batched: one resident batch; loop: the same scenes as resident single-scene batches; "
                     "advance loop: one drop-in solver per scene, advance() with host arrays every frame"}
 
@@ -278,6 +358,7 @@ def bench_large(params, steps=20, warmup=3, tune=True):
         for i, v in enumerate(batch.stage_times()):
             stage_sum[i] += v
     flags = batch.error_flags()
+    surface = time_surface(batch, stream)  # the 512x256x256-cell lattice
     batch.close()
     solver.close()
     ms = total_ms / steps
@@ -290,7 +371,7 @@ def bench_large(params, steps=20, warmup=3, tune=True):
     return {"workload": "double_dam_8m", "particles": n, "steps": steps, "warmup": warmup,
             "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3), "stages_ms_per_step": stages,
             "step_algorithmic_bytes": algo, "step_achieved_gbs": gbs, "hbm_peak_gbs": peak,
-            "hbm_peak_kind": peak_kind, "step_hbm_frac": gbs / peak, "error_flags": flags,
+            "hbm_peak_kind": peak_kind, "step_hbm_frac": gbs / peak, "error_flags": flags, "surface": surface,
             "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3)} if tuned else None)}
 
 
@@ -333,10 +414,13 @@ def bench_ref_profile(steps=30, warmup=5, tune=True):
             "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3), "error_flags": flags}
 
 
-def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=0):
-    """Workload 5: saturation throughput, then a Poisson stream at 80% of it."""
+def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=0, log_path=None, rank=0, world=1):
+    """Workload 5: saturation throughput, then a Poisson stream at 80% of it.  With
+    several ranks every rank draws the same streams and serves the requests a
+    replicated Router gives it (partition.route_stream): the job's throughput is the
+    ranks' particle-steps over the slowest rank's time, latencies are pooled."""
     import numpy as np
-    from libfluid_gb300 import scenes
+    from libfluid_gb300 import partition, scenes
     from libfluid_gb300.serve import Server
     from libfluid_gb300.solver import SphSolver
     cache = {}
@@ -349,12 +433,14 @@ def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=
     stream = scenes.serving_stream(requests, 1.0, seed=seed)
     work = [(n, st, mesh) for _, n, st, mesh, _ in stream]
     mean_ps = float(np.mean([n * st for n, st, _ in work]))
+    mine = [w for _, w in partition.route_stream(work, rank, world, n_of=lambda w: w[0], steps_of=lambda w: w[1])]
     solver = SphSolver(params=params)
 
     def saturate(one_at_a_time):
         sv = Server(solver, one_at_a_time=one_at_a_time, tick_particles=tick_particles)
+        partition.barrier()
         tickets = []
-        for n, st, mesh in work:
+        for n, st, mesh in mine:
             p, c = scene_for(n)
             tickets.append(sv.submit(c, p, st, mesh))
         sv.drain(1200)
@@ -362,18 +448,23 @@ def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=
         for t in tickets:
             sv.fetch(t)
         sv.close()
-        return s.particle_steps / s.elapsed_seconds, s
+        return s
 
-    sat, s_sat = saturate(False)
-    loop, _ = saturate(True)
+    s_sat = saturate(False)
+    s_loop = saturate(True)
+    sat_all = partition.gather_summary((s_sat.particle_steps, s_sat.elapsed_seconds, s_loop.particle_steps,
+                                        s_loop.elapsed_seconds))
+    sat = sum(x[0] for x in sat_all) / max(x[1] for x in sat_all)
+    loop = sum(x[2] for x in sat_all) / max(x[3] for x in sat_all)
     rate = 0.8 * sat / mean_ps
     arrivals = scenes.serving_stream(100000, rate, seed=seed + 1)
+    arrivals = [a for a in arrivals if a[0] <= run_seconds]
+    mine_arr = [a for _, a in partition.route_stream(arrivals, rank, world)]
     sv = Server(solver, tick_particles=tick_particles)
+    partition.barrier()
     t0 = time.perf_counter()
     tickets = []
-    for t_arr, n, st, mesh, _ in arrivals:
-        if t_arr > run_seconds:
-            break
+    for t_arr, n, st, mesh, _ in mine_arr:
         delay = t_arr - (time.perf_counter() - t0)
         if delay > 0:
             time.sleep(delay)
@@ -382,21 +473,54 @@ def bench_serving(params, requests=48, run_seconds=25.0, seed=5, tick_particles=
     sv.drain(1200)
     res = [sv.poll(t) for t in tickets]
     lat = sv.step_latencies()
+    tick_scenes = sv.tick_scenes()
+    tick_parts = sv.tick_particles()
+    tick_starts = sv.tick_starts()
+    tick_steps = sv.tick_steps()
     s = sv.stats()
     for t in tickets:
         sv.fetch(t)
     sv.close()
     solver.close()
     req = np.array([r.t_done - r.t_submit for r in res if r.status == 2])
+    if log_path and rank == 0:
+        np.savez(log_path, latency=lat, scenes=tick_scenes, particles=tick_parts, starts=tick_starts,
+                 steps=tick_steps, request_latency=req)
+    # the latency each request saw for its next state: every request of a tick waits
+    # that tick's time (a tick of k steps hands over k steps at once)
+    per_req = np.repeat(lat, tick_scenes[:len(lat)]) if len(tick_scenes) >= len(lat) else lat
+    # time per request-step: a tick's time over the steps it advanced
+    per_step = np.repeat(lat / np.maximum(tick_steps[:len(lat)], 1), tick_scenes[:len(lat)])
+    pooled = partition.gather_summary({"lat": lat, "req": req, "per_req": per_req, "per_step": per_step,
+                                       "ticks_steps": tick_steps, "requests": len(tickets),
+                                       "completed": int(s.completed), "particle_steps": s.particle_steps,
+                                       "elapsed": s.elapsed_seconds, "rebuilds": int(s.rebuilds),
+                                       "rebuild_s": s.rebuild_seconds, "sat_rebuilds": int(s_sat.rebuilds)})
+    lat = np.concatenate([p["lat"] for p in pooled])
+    req = np.concatenate([p["req"] for p in pooled])
+    per_req = np.concatenate([p["per_req"] for p in pooled])
+    per_step = np.concatenate([p["per_step"] for p in pooled])
+    ks = np.concatenate([p["ticks_steps"] for p in pooled])
     pct = lambda a, q: float(np.percentile(a, q)) * 1e3 if len(a) else None  # noqa: E731
-    return {"workload": "serving", "saturation_particle_steps_per_s": sat,
+    return {"workload": "serving", "ranks": world, "saturation_particle_steps_per_s": sat,
             "one_at_a_time_particle_steps_per_s": loop, "batching_gain": sat / loop,
-            "offered_fraction_of_saturation": 0.8, "arrival_rate_per_s": rate, "requests": len(tickets),
-            "completed": int(s.completed), "particle_steps_per_s": s.particle_steps / s.elapsed_seconds,
+            "offered_fraction_of_saturation": 0.8, "arrival_rate_per_s": rate,
+            "requests": sum(p["requests"] for p in pooled), "completed": sum(p["completed"] for p in pooled),
+            "particle_steps_per_s": sum(p["particle_steps"] for p in pooled) / max(p["elapsed"] for p in pooled),
             "step_ms": {"p50": pct(lat, 50), "p95": pct(lat, 95), "p99": pct(lat, 99)},
             "request_ms": {"p50": pct(req, 50), "p95": pct(req, 95), "p99": pct(req, 99)},
             "p99_over_p50_step": (pct(lat, 99) / pct(lat, 50)) if len(lat) else None,
-            "rebuilds": int(s.rebuilds), "rebuild_s": s.rebuild_seconds, "saturation_rebuilds": int(s_sat.rebuilds)}
+            "request_step_ms": {"p50": pct(per_req, 50), "p95": pct(per_req, 95), "p99": pct(per_req, 99)},
+            "p99_over_p50_request_step": (pct(per_req, 99) / pct(per_req, 50)) if len(per_req) else None,
+            "steps_per_tick": {"mean": float(ks.mean()) if len(ks) else None,
+                               "max": int(ks.max()) if len(ks) else None,
+                               "multi_step_fraction": float((ks > 1).mean()) if len(ks) else None},
+            "per_step_ms": {"p50": pct(per_step, 50), "p95": pct(per_step, 95), "p99": pct(per_step, 99)},
+            "latency_note": "step_ms: tick latency, the time a request waits for its next state (a tick "
+                            "advances its group by one step, or by several when the group holds less than "
+                            "half the tick budget); per_step_ms: that time over the steps the tick advanced",
+            "rebuilds": sum(p["rebuilds"] for p in pooled), "rebuild_s": sum(p["rebuild_s"] for p in pooled),
+            "saturation_rebuilds": sum(p["sat_rebuilds"] for p in pooled)}
 
 
 REF_ARM_BUDGET_S = 150.0  # wall time the reference arm's timed steps may take
@@ -481,6 +605,7 @@ def run_ours(args):
     build.build()
     params = capi.params(capi.PROFILE_BASELINE, 0.1)
     parts, cfg = scenes.dam_break_1m()
+    parts0 = scenes.copy_particles(parts)  # the initial state, for the full-run and drop-in legs
     n = len(parts["mass"])
     solver = SphSolver(params=params)
     # a dedicated (non-legacy) stream: the library launches its graphs on it and the
@@ -584,15 +709,61 @@ def run_ours(args):
     e2e_value = n * e2e_steps * world / float(te.item())
     e2e_solver.close()
 
+    # the 200-step run of the workload as stated, from the initial state: every step
+    # device-resident (no L2 flush: one continuous run), then the end-of-run surface
+    # of the 256x128x128-cell lattice; and the same 200 frames through fgb_advance
+    full_run = None
+    if world == 1 and not args.no_extra:
+        full_steps = 200
+        fb = Batch(solver, [(scenes.copy_particles(parts0), cfg)])
+        fb.sync()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        fb.step(full_steps)
+        f1.record(stream)
+        f1.synchronize()
+        dev_ms = f0.elapsed_time(f1) / full_steps
+        surface = time_surface(fb, stream)
+        ff = fb.error_flags()
+        fb.close()
+        host_full = scenes.copy_particles(parts0)
+        fs = SphSolver(params=params)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(full_steps):
+            fs.advance(cfg, host_full)
+        e2e_full_s = time.perf_counter() - t0
+        fs.close()
+        full_run = {"steps": full_steps, "device_ms_per_step": dev_ms,
+                    "device_particle_steps_per_s": n / (dev_ms * 1e-3),
+                    "e2e_ms_per_frame": 1e3 * e2e_full_s / full_steps,
+                    "e2e_particle_steps_per_s": n * full_steps / e2e_full_s, "error_flags": ff,
+                    "surface_end_of_run": surface}
+
+    # the drop-in as an application calls it: cuda::SphSolver::advance on a
+    # std::vector<fluid::Particle>, the same window as e2e (W frames, then K timed)
+    dropin = None
+    if rank == 0 and world == 1 and not args.no_extra:
+        d = dropin_frames(parts0, cfg, args.warmup, args.steps)
+        if "ms_per_frame" in d:
+            dropin = {"value": n / (d["ms_per_frame"] * 1e-3), "unit": UNIT, "ms_per_frame": d["ms_per_frame"],
+                      "frames": d["frames"], "call": "cuda::SphSolver::advance (C++, std::vector<fluid::Particle>)",
+                      "vs_e2e": (n / (d["ms_per_frame"] * 1e-3)) / e2e_value}
+        else:
+            dropin = d
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(args.cpu_seconds, params, scenes.dam_break_1m)
     batched = serving = large = ref_profile = None
-    if world == 1 and not args.no_extra:
-        batched = bench_batched(params, tune=not args.no_tune)
-        large = bench_large(params, tune=not args.no_tune)
-        ref_profile = bench_ref_profile(tune=not args.no_tune)
-        serving = bench_serving(params)
+    if not args.no_extra:
+        # the scene-sharded legs run on every rank (each its share); the single-scene
+        # legs on one GPU
+        batched = bench_batched(params, tune=not args.no_tune, rank=rank, world=world)
+        if world == 1:
+            large = bench_large(params, tune=not args.no_tune)
+            ref_profile = bench_ref_profile(tune=not args.no_tune)
+        serving = bench_serving(params, log_path=args.serving_log, rank=rank, world=world)
 
     if rank == 0:
         line = {
@@ -617,6 +788,8 @@ def run_ours(args):
             "stages_ms_per_step": {nm: round(v[0] / args.steps, 4) for nm, v in per_kernel.items()},
             "stage_sum_ms_per_step": step_total,
             "cpu_baseline": cpu,
+            "e2e_dropin": dropin,
+            "full_run": full_run,
             "clocks": clk,
             "gpu_launches": launches,
             "error_flags": flags,
@@ -662,6 +835,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and serving legs")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default launch shapes)")
+    ap.add_argument("--serving-log", default=None,
+                    help="write the serving leg's tick log (latency, scenes, particles, start) to this .npz")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run 4 untimed steps of the workload and exit (the case that ncu captures)")
     ap.add_argument("--ncu-profile", default="baseline", choices=["baseline", "ref"],

@@ -115,6 +115,31 @@ typedef struct fgb_mesh {
     size_t capacity;
 } fgb_mesh;
 
+/* A query point and its result (fluid::Query, fluid::QueryResult: fluid.hpp:21-49). */
+typedef struct fgb_query {
+    uint64_t id;
+    float point[3];     /* world units */
+} fgb_query;
+typedef struct fgb_query_result {
+    uint64_t id;
+    float point[3];
+    uint64_t neighbours;      /* fluid particles in the point's grid cell */
+    uint32_t average_colour;  /* their mean ARGB colour, each channel truncated */
+} fgb_query_result;
+
+/* The caller's array of particle records, e.g. std::vector<fluid::Particle<size_t,
+ * float>> (fluid.hpp:52-62), read and written in place: field f of record i lies at
+ * base + i * stride + f.  Offsets are bytes within a record (multiples of 4); id and
+ * colour may be -1 (absent: the index, and 0xffffffff).  type holds FGB_TYPE_* as a
+ * 4-byte integer (the fluid::Type enum); position and velocity are three floats. */
+typedef struct fgb_records {
+    void *base;
+    size_t n;
+    uint32_t stride;      /* bytes from one record to the next: a multiple of 4, at most 128 */
+    uint32_t id_bytes;    /* 8 (size_t ids) or 4 */
+    int32_t id, type, mass, position, velocity, colour;
+} fgb_records;
+
 typedef struct fgb_solver fgb_solver;
 typedef struct fgb_batch fgb_batch;
 typedef struct fgb_server fgb_server;
@@ -126,7 +151,7 @@ const char *fgb_last_error(void);
 /* sizeof of the ABI structs in this order: fgb_params, fgb_config, fgb_particles,
  * fgb_triangle, fgb_mesh_triangle, fgb_mesh, fgb_grid_info, fgb_well,
  * fgb_serve_options, fgb_serve_result, fgb_serve_stats, fgb_tune_result, fgb_source,
- * fgb_drain; writes at most
+ * fgb_drain, fgb_query, fgb_query_result, fgb_records; writes at most
  * n values and returns how many exist.  Replaces the reference's check_size kernel
  * and host assert of struct layouts (oclsph_kernel.h:276-278, oclsph.hpp:217-243). */
 int fgb_struct_sizes(uint64_t *out, int n);
@@ -149,6 +174,19 @@ int fgb_set_stream(fgb_solver *s, void *cuda_stream);
 int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs,
                 const fgb_triangle *colliders, size_t n_colliders, fgb_mesh *mesh_out);
 void fgb_mesh_free(fgb_mesh *m);
+/* The reference's advance in full (oclsph.hpp:661-936) on the caller's array of
+ * records, read and written in place (reordered into Morton order like fgb_advance),
+ * with the frame's cell queries (oclsph.hpp:770-791): each query point's cell in the
+ * step's grid (of the predicted positions), the fluid particles in it and their mean
+ * colour before the step's colour diffusion; results only for points whose cell holds
+ * fluid, in query order, *n_results of them (results must hold n_queries).  A point
+ * outside the grid has no result.  Where the device addresses the records directly
+ * (a coherent link) kernels read and write them; elsewhere the host threads pack them.
+ * mesh_out as in fgb_advance. */
+int fgb_advance_records(fgb_solver *s, const fgb_config *cfg, fgb_records *xs,
+                        const fgb_triangle *colliders, size_t n_colliders,
+                        const fgb_query *queries, size_t n_queries,
+                        fgb_query_result *results, size_t *n_results, fgb_mesh *mesh_out);
 /* Give every page of the host range [p, p + bytes) that is not resident a frame
  * before kernels address it over a coherent link (what fgb_advance and the direct
  * downloads do to the caller's arrays): a GPU store into a page the host never wrote
@@ -191,6 +229,16 @@ int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
 int fgb_batch_sync(fgb_batch *b);
 /* Device error flags raised by bounded waits since the last call (0: none). */
 int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags);
+/* The shared-memory halo of the gather kernels at the last step: CTAs of the step
+ * and how many of them read their neighbours from shared memory (the rest read
+ * global memory: their particles span two scenes or their box is too large).  Both
+ * 0 when the batch runs without the halo.  Synchronous; changes no result. */
+int fgb_batch_halo_usage(fgb_batch *b, uint32_t *ctas, uint32_t *halo_ctas);
+/* With FGB_ROW_STATS=1 in the environment when the batch is created: warps of the
+ * checked neighbour passes (later lambda passes, the vorticity pass) that ran on
+ * their near rows and warps that filtered their candidates instead, summed over the
+ * steps since the last call (which clears them); both 0 otherwise.  Synchronous. */
+int fgb_batch_row_stats(fgb_batch *b, uint32_t *near_warps, uint32_t *filter_warps);
 /* Number of kernels this batch launched since creation (for accounting). */
 uint64_t fgb_batch_launch_count(const fgb_batch *b);
 /* Stage timing (replaces the reference's DEBUG-only clutil::Stopwatch phases,
@@ -244,6 +292,11 @@ typedef struct fgb_grid_info {
     float lattice_step;       /* solver units */
 } fgb_grid_info;
 int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out);
+/* Cell queries of a resident scene against the grid of the batch's last
+ * fgb_batch_step, as fgb_advance_records answers them; FGB_ERR_INVALID when an upload,
+ * an edit or a surface since the step replaced that grid. */
+int fgb_batch_query(fgb_batch *b, uint32_t scene, const fgb_query *queries, size_t n,
+                    fgb_query_result *results, size_t *n_results);
 /* Copy resident scene src_scene of src into dst_scene of dst on the device (same
  * particle count, same solver).  The particle order is kept, so the scene's later
  * steps are bit-identical to what src would have computed. */
@@ -294,6 +347,10 @@ typedef struct fgb_serve_options {
     uint32_t one_at_a_time;  /* 1: no batching, one scene at a time (the comparison loop) */
     uint64_t tick_particles; /* most particles stepped in one tick (0: 2 097 152); a
                                 larger scene is stepped alone */
+    uint32_t max_steps_per_tick; /* a group below half of tick_particles is advanced
+                                    several steps in one tick, so that every tick does
+                                    about a full group's work: at most this many (0: 16;
+                                    1: one step per tick); one_at_a_time takes one */
 } fgb_serve_options;
 
 typedef struct fgb_serve_result {
@@ -323,6 +380,12 @@ int fgb_serve_get_stats(fgb_server *sv, fgb_serve_stats *out);
 int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
 /* Particles stepped by every tick, in the order of fgb_serve_step_latencies. */
 int fgb_serve_tick_particles(fgb_server *sv, uint64_t *out, uint64_t max, uint64_t *count);
+/* Requests stepped by every tick, in the same order: each of them saw a step of that
+ * tick's latency (the latency a request sees per step is the tick's, weighted by
+ * these counts). */
+int fgb_serve_tick_scenes(fgb_server *sv, uint32_t *out, uint64_t max, uint64_t *count);
+/* Steps every tick advanced its group by, in the same order. */
+int fgb_serve_tick_steps(fgb_server *sv, uint32_t *out, uint64_t max, uint64_t *count);
 /* Start of every tick in seconds since fgb_serve_create, in the same order. */
 int fgb_serve_tick_starts(fgb_server *sv, double *out, uint64_t max, uint64_t *count);
 int fgb_serve_drain(fgb_server *sv, double timeout_seconds);

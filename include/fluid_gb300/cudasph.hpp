@@ -6,15 +6,18 @@
 // "fluid_gb300/compat/fluid.hpp" first; then this header; link libfluidgb.so.
 //
 // What stays on the host, as in the reference's advance: sources and drains
-// (oclsph.hpp:675-708) and query results (oclsph.hpp:770-791).  Everything else --
-// prediction, the Morton grid, the constraint iterations, the velocity update and
-// marching cubes -- runs on the GPU through the C ABI in fluid_gb300.h.  Failures
+// (oclsph.hpp:675-708), which resize the vector.  Everything else -- the particles'
+// upload and write-back (read and written in place in the vector), prediction, the
+// Morton grid, the constraint iterations, the velocity update, the cell queries
+// (oclsph.hpp:770-791) and marching cubes -- runs on the GPU through the C ABI in
+// fluid_gb300.h.  Failures
 // throw std::runtime_error carrying the library's message, as the reference throws.
 #ifndef FLUID_GB300_CUDASPH_HPP
 #define FLUID_GB300_CUDASPH_HPP
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -40,33 +43,38 @@ public:
 
     fgb_solver *handle() const { return solver_; }
 
+    // An analytic static sphere collider (world units) for the frames that follow;
+    // radius <= 0 removes it.  No counterpart in fluid::Config, whose colliders are
+    // triangle meshes: the benchmark's 1M dam break has a sphere.
+    void sphere(float cx, float cy, float cz, float radius) {
+        sphere_[0] = cx;
+        sphere_[1] = cy;
+        sphere_[2] = cz;
+        sphere_[3] = radius;
+    }
+
     fluid::Result<float> advance(const fluid::Config<float> &config, std::vector<fluid::Particle<size_t, float>> &xs,
                                  const std::vector<fluid::MeshCollider<float>> &colliders) override {
         emit_sources(config, xs);
         apply_drains(config, xs);
         if (xs.empty()) return fluid::Result<float>({}, {});  // oclsph.hpp:711-715
 
-        const size_t n = xs.size();
-        id_.resize(n);
-        type_.resize(n);
-        mass_.resize(n);
-        colour_.resize(n);
-        pos_.resize(3 * n);
-        vel_.resize(3 * n);
-        for (size_t i = 0; i < n; ++i) {
-            const auto &p = xs[i];
-            id_[i] = (uint64_t)p.id;
-            type_[i] = p.type == fluid::Type::Obstacle ? FGB_TYPE_OBSTACLE : FGB_TYPE_FLUID;
-            mass_[i] = p.mass;
-            colour_[i] = p.colour;
-            pos_[3 * i] = p.position.x;
-            pos_[3 * i + 1] = p.position.y;
-            pos_[3 * i + 2] = p.position.z;
-            vel_[3 * i] = p.velocity.x;
-            vel_[3 * i + 1] = p.velocity.y;
-            vel_[3 * i + 2] = p.velocity.z;
-        }
-        fgb_particles view{n, id_.data(), type_.data(), mass_.data(), pos_.data(), vel_.data(), colour_.data()};
+        // the particles are read and written where they lie: the library addresses the
+        // vector's records through their field offsets (no copy into separate arrays)
+        using P = fluid::Particle<size_t, float>;
+        static_assert(sizeof(fluid::Type) == 4, "fluid::Type must be a 4-byte enum");
+        static_assert(sizeof(P) % 4 == 0 && sizeof(P) <= 128, "fluid::Particle layout");
+        fgb_records view;
+        view.base = xs.data();
+        view.n = xs.size();
+        view.stride = (uint32_t)sizeof(P);
+        view.id_bytes = (uint32_t)sizeof(size_t);
+        view.id = (int32_t)offsetof(P, id);
+        view.type = (int32_t)offsetof(P, type);
+        view.mass = (int32_t)offsetof(P, mass);
+        view.position = (int32_t)offsetof(P, position);
+        view.velocity = (int32_t)offsetof(P, velocity);
+        view.colour = (int32_t)offsetof(P, colour);
 
         fgb_config c;
         fgb_config_default(&c, FGB_PROFILE_REF);
@@ -85,6 +93,8 @@ public:
         c.max_bound[0] = config.maxBound.x;
         c.max_bound[1] = config.maxBound.y;
         c.max_bound[2] = config.maxBound.z;
+        c.sphere_enabled = sphere_[3] > 0.f ? 1 : 0;
+        for (int a = 0; a < 4; ++a) c.sphere[a] = sphere_[a];
         if (config.wells.size() > FGB_MAX_WELLS) throw std::runtime_error("libfluidgb: more than 16 wells");
         c.n_wells = (uint32_t)config.wells.size();
         for (size_t w = 0; w < config.wells.size(); ++w) {
@@ -98,21 +108,32 @@ public:
             for (const auto &t : m.triangles)
                 tris_.push_back(fgb_triangle{{t.v0.x, t.v0.y, t.v0.z}, {t.v1.x, t.v1.y, t.v1.z}, {t.v2.x, t.v2.y, t.v2.z}});
 
+        // queries of the frame (oclsph.hpp:770-791), answered on the device from the
+        // step's grid
+        queries_.resize(config.queries.size());
+        for (size_t q = 0; q < config.queries.size(); ++q) {
+            queries_[q].id = (uint64_t)config.queries[q].id;
+            queries_[q].point[0] = config.queries[q].point.x;
+            queries_[q].point[1] = config.queries[q].point.y;
+            queries_[q].point[2] = config.queries[q].point.z;
+        }
+        results_.resize(queries_.size());
+        size_t n_results = 0;
         fgb_mesh mesh{nullptr, 0, 0};
-        int rc = fgb_advance(solver_, &c, &view, tris_.empty() ? nullptr : tris_.data(), tris_.size(), &mesh);
+        // the library writes the particles back in Morton order (oclsph.hpp:875-891)
+        int rc = fgb_advance_records(solver_, &c, &view, tris_.empty() ? nullptr : tris_.data(), tris_.size(),
+                                     queries_.empty() ? nullptr : queries_.data(), queries_.size(),
+                                     results_.empty() ? nullptr : results_.data(), &n_results, &mesh);
         if (rc != FGB_OK) {
             fgb_mesh_free(&mesh);
             throw std::runtime_error(std::string("libfluidgb: ") + fgb_last_error());
         }
-        // write-back in Morton order (oclsph.hpp:875-891)
-        for (size_t i = 0; i < n; ++i) {
-            auto &p = xs[i];
-            p.id = (size_t)id_[i];
-            p.type = type_[i] == FGB_TYPE_OBSTACLE ? fluid::Type::Obstacle : fluid::Type::Fluid;
-            p.mass = mass_[i];
-            p.colour = colour_[i];
-            p.position = fluid::tvec3<float>(pos_[3 * i], pos_[3 * i + 1], pos_[3 * i + 2]);
-            p.velocity = fluid::tvec3<float>(vel_[3 * i], vel_[3 * i + 1], vel_[3 * i + 2]);
+        std::vector<fluid::QueryResult<float>> query_results;
+        query_results.reserve(n_results);
+        for (size_t q = 0; q < n_results; ++q) {
+            const fgb_query_result &r = results_[q];
+            query_results.emplace_back((size_t)r.id, fluid::tvec3<float>(r.point[0], r.point[1], r.point[2]),
+                                       (size_t)r.neighbours, r.average_colour);
         }
         std::vector<geometry::MeshTriangle<float>> triangles(mesh.n);
         for (size_t t = 0; t < mesh.n; ++t) {
@@ -129,17 +150,16 @@ public:
             o.c.z = m.c[2];
         }
         fgb_mesh_free(&mesh);
-        return fluid::Result<float>(triangles, queries(config, xs));
+        return fluid::Result<float>(triangles, query_results);
     }
 
 private:
     fgb_solver *solver_ = nullptr;
     float h_ = 0.1f;
-    std::vector<uint64_t> id_;
-    std::vector<int32_t> type_;
-    std::vector<float> mass_, pos_, vel_;
-    std::vector<uint32_t> colour_;
+    float sphere_[4] = {0.f, 0.f, 0.f, 0.f};
     std::vector<fgb_triangle> tris_;
+    std::vector<fgb_query> queries_;
+    std::vector<fgb_query_result> results_;
 
     void init(const fgb_params &p) {
         h_ = p.h;
@@ -173,40 +193,6 @@ private:
                                     return false;
                                 }),
                  xs.end());
-    }
-
-    // oclsph.hpp:770-791: fluid particles in the query point's grid cell and their
-    // mean ARGB colour (here over the advanced positions)
-    std::vector<fluid::QueryResult<float>> queries(const fluid::Config<float> &config,
-                                                   const std::vector<fluid::Particle<size_t, float>> &xs) const {
-        std::vector<fluid::QueryResult<float>> out;
-        if (config.queries.empty()) return out;
-        const float pad = h_ * 2.f;
-        const float mn[3] = {config.minBound.x / config.scale - pad, config.minBound.y / config.scale - pad,
-                             config.minBound.z / config.scale - pad};
-        auto cell = [&](const fluid::tvec3<float> &p, long c[3]) {
-            const float v[3] = {p.x / config.scale, p.y / config.scale, p.z / config.scale};
-            for (int a = 0; a < 3; ++a) c[a] = (long)std::floor((v[a] - mn[a]) / h_);
-        };
-        for (const auto &q : config.queries) {
-            long qc[3];
-            cell(q.point, qc);
-            size_t count = 0;
-            double acc[4] = {0, 0, 0, 0};
-            for (const auto &p : xs) {
-                if (p.type != fluid::Type::Fluid) continue;
-                long pc[3];
-                cell(p.position, pc);
-                if (pc[0] != qc[0] || pc[1] != qc[1] || pc[2] != qc[2]) continue;
-                ++count;
-                for (int ch = 0; ch < 4; ++ch) acc[ch] += (double)((p.colour >> (24 - 8 * ch)) & 0xffu);
-            }
-            if (!count) continue;
-            uint32_t argb = 0;
-            for (int ch = 0; ch < 4; ++ch) argb |= ((uint32_t)(acc[ch] / (double)count) & 0xffu) << (24 - 8 * ch);
-            out.emplace_back(q.id, q.point, count, argb);
-        }
-        return out;
     }
 };
 

@@ -13,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfluidgb.so")
-SOURCES = ["sort.cu", "scan.cu", "pbf.cu", "mc.cu", "runtime.cu", "serve.cu", "wire.cu", "weld.cu", "edit.cu", "hostio.cu"]
+SOURCES = ["sort.cu", "scan.cu", "pbf.cu", "mc.cu", "runtime.cu", "serve.cu", "wire.cu", "weld.cu", "edit.cu", "hostio.cu",
+           "query.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
          "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",

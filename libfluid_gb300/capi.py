@@ -134,6 +134,7 @@ class ServeOptions(ctypes.Structure):
         ("max_active", ctypes.c_uint32),
         ("one_at_a_time", ctypes.c_uint32),
         ("tick_particles", ctypes.c_uint64),
+        ("max_steps_per_tick", ctypes.c_uint32),
     ]
 
 
@@ -177,6 +178,57 @@ class Drain(ctypes.Structure):
     _fields_ = [("centre", f3), ("width", ctypes.c_float), ("depth", ctypes.c_float)]
 
 
+class Query(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("point", ctypes.c_float * 3)]
+
+
+class QueryResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("point", ctypes.c_float * 3), ("neighbours", ctypes.c_uint64),
+                ("average_colour", ctypes.c_uint32)]
+
+
+class Records(ctypes.Structure):
+    _fields_ = [("base", ctypes.c_void_p), ("n", ctypes.c_size_t), ("stride", ctypes.c_uint32),
+                ("id_bytes", ctypes.c_uint32), ("id", ctypes.c_int32), ("type", ctypes.c_int32),
+                ("mass", ctypes.c_int32), ("position", ctypes.c_int32), ("velocity", ctypes.c_int32),
+                ("colour", ctypes.c_int32)]
+
+
+# numpy record type with the layout of fluid::Particle<size_t, float> (fluid.hpp:52-62)
+# built against GLM's packed vectors: id, type, mass, position, velocity, colour
+PARTICLE_RECORD = np.dtype({"names": ["id", "type", "mass", "position", "velocity", "colour"],
+                            "formats": [np.uint64, np.int32, np.float32, (np.float32, 3), (np.float32, 3), np.uint32],
+                            "offsets": [0, 8, 12, 16, 28, 40], "itemsize": 48})
+
+
+def records_view(rec):
+    """Records struct over a numpy array of PARTICLE_RECORD (kept alive by the caller)."""
+    r = Records()
+    r.base = rec.ctypes.data
+    r.n = len(rec)
+    r.stride = rec.dtype.itemsize
+    r.id_bytes = 8
+    f = rec.dtype.fields
+    r.id, r.type, r.mass = f["id"][1], f["type"][1], f["mass"][1]
+    r.position, r.velocity, r.colour = f["position"][1], f["velocity"][1], f["colour"][1]
+    return r
+
+
+def to_records(parts):
+    n = len(parts["mass"])
+    rec = np.zeros(n, PARTICLE_RECORD)
+    rec["id"], rec["type"], rec["mass"], rec["colour"] = parts["id"], parts["type"], parts["mass"], parts["colour"]
+    rec["position"] = parts["position"].reshape(n, 3)
+    rec["velocity"] = parts["velocity"].reshape(n, 3)
+    return rec
+
+
+def from_records(rec):
+    return {"id": rec["id"].copy(), "type": rec["type"].copy(), "mass": rec["mass"].copy(),
+            "position": np.ascontiguousarray(rec["position"]).ravel().copy(),
+            "velocity": np.ascontiguousarray(rec["velocity"]).ravel().copy(), "colour": rec["colour"].copy()}
+
+
 class TuneResult(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("skin", ctypes.c_float), ("ms_per_step", ctypes.c_float),
                 ("trials", ctypes.c_uint32), ("steps", ctypes.c_uint32)]
@@ -207,6 +259,8 @@ _SIGS = {
     "fgb_batch_surface_fetch": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(Mesh)]),
     "fgb_batch_sync": (ctypes.c_int, [c_void_p]),
     "fgb_batch_error_flags": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
+    "fgb_batch_halo_usage": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), P(ctypes.c_uint32)]),
+    "fgb_batch_row_stats": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), P(ctypes.c_uint32)]),
     "fgb_batch_host_io": (ctypes.c_int, [c_void_p, P(ctypes.c_int)]),
     "fgb_batch_prepare": (ctypes.c_int, [c_void_p]),
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),
@@ -232,6 +286,10 @@ _SIGS = {
                                                 P(ctypes.c_uint64)]),
     "fgb_serve_tick_starts": (ctypes.c_int, [c_void_p, P(ctypes.c_double), ctypes.c_uint64,
                                              P(ctypes.c_uint64)]),
+    "fgb_serve_tick_scenes": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), ctypes.c_uint64,
+                                             P(ctypes.c_uint64)]),
+    "fgb_serve_tick_steps": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), ctypes.c_uint64,
+                                            P(ctypes.c_uint64)]),
     "fgb_serve_drain": (ctypes.c_int, [c_void_p, ctypes.c_double]),
     "fgb_serve_destroy": (ctypes.c_int, [c_void_p]),
     "fgb_exclusive_scan_u32_noalloc": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, ctypes.c_uint64, c_void_p]),
@@ -255,6 +313,10 @@ _SIGS = {
     "fgb_scan_noalloc_error": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
     "fgb_test_lookback_fault": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32]),
     "fgb_host_ready_pages": (ctypes.c_int, [c_void_p, ctypes.c_size_t, ctypes.c_int, P(ctypes.c_uint64)]),
+    "fgb_advance_records": (ctypes.c_int, [c_void_p, P(Config), P(Records), P(Triangle), ctypes.c_size_t, P(Query),
+                                           ctypes.c_size_t, P(QueryResult), P(ctypes.c_size_t), P(Mesh)]),
+    "fgb_batch_query": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(Query), ctypes.c_size_t, P(QueryResult),
+                                       P(ctypes.c_size_t)]),
 }
 
 _lib = None

@@ -1,8 +1,9 @@
 // fgb_device.cuh -- device-side building blocks shared by the PBF and MC kernels.
 //
-// All float arithmetic on the parity path is written with an explicit operation
-// order: the library is compiled with -fmad=false, and fused multiply-adds appear
-// only as __fmaf_rn where the CPU oracle uses fmaf, so both sides round alike.
+// All float arithmetic is written with an explicit operation order: the library is
+// compiled with -fmad=false, and fused multiply-adds appear only as __fmaf_rn, so a
+// kernel computes the same bits on every code path that evaluates the same sum.
+// Where the CPU oracle uses fmaf the kernels do too, so the two round alike.
 #pragma once
 
 #include <cstdint>

@@ -70,7 +70,10 @@ struct StepView {
     float skin;            // a list stays exact while disp_a + max disp_b <= skin
     float4 *ps_grid;       // p* at grid build (displacements are measured from it)
     float *disp;           // |p - p_grid| per particle after the last delta pass
-    uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
+    float *dstep;          // distance moved by the last delta pass, per particle
+    // per cell (same index as cells), float bits: {max disp, max dstep} of the last
+    // delta pass over the cell's particles
+    uint2 *cellmax;
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
     // per-pass hit lists: the candidates of one pass that lie within h (and not on top
     // of the particle), in walk order; written by a lambda / vorticity pass, read by the
@@ -78,9 +81,12 @@ struct StepView {
     uint32_t *hlist;       // n * hcap
     uint16_t *hcount;      // entries per particle (kListOverflow: use nlist / the cells)
     uint32_t hcap;
-    // near rows: the build pass's hit row keeps every candidate within h + near_skin;
-    // near[a] = 1 while particle a's row is that row (null: near rows off)
+    // near rows: a hit row that keeps every candidate within h + near_skin of the
+    // positions of the pass that wrote it; near[a] = 1 while particle a's row is such
+    // a row, and slack[a] bounds how far a and its candidates have moved since
+    // (null: near rows off)
     uint8_t *near;
+    float *slack;
     float near_r2;         // (h + near_skin)^2, rounded up
     float near_skin;
     // the step's last kernel also stores each particle's final position and velocity
@@ -88,7 +94,22 @@ struct StepView {
     const HostParticlesOut *hout;
     // the build pass counts the Verlet rows [0] and hit rows [1] that overflowed
     uint32_t *over;
+    // null, or [0] warps of the checked passes that ran on their near rows and [1]
+    // warps that filtered their candidates instead (accumulated until read)
+    uint32_t *near_stats;
+    // shared-memory halo of every CTA of halo_threads() particles (pbf.cu; null: off)
+    void *halo_hdr;
+    uint2 *halo_box;
 };
+
+// the shared-memory halo of the gathers (pbf.cu): bytes of its per-step arrays for n
+// particles, the CTA size it needs, and the kernel attributes it sets once per device
+uint64_t halo_header_bytes(uint64_t n);
+uint64_t halo_box_bytes(uint64_t n);
+uint32_t halo_threads();
+// CTAs in halo mode among `ctas` headers copied to the host
+uint32_t halo_count(const void *host_headers, uint64_t ctas);
+cudaError_t halo_setup();
 
 constexpr uint16_t kListOverflow = 0xffffu;
 
@@ -153,7 +174,31 @@ struct HostParticlesOut {  // any may be null: not written
     int32_t *type;
     uint32_t *colour;
     uint64_t *id;
+    // 0: the arrays above are packed (structure of arrays).  Otherwise they address
+    // the fields of record 0 of the caller's array of records, record i's fields sit
+    // i * stride bytes further, and the id field is id_bytes (4 or 8) wide
+    uint32_t stride = 0, id_bytes = 8;
 };
+// The caller's array of records (e.g. fluid::Particle): field f of record i at
+// base + i * stride + off_f; a negative offset marks an absent field (colour: all
+// ones, id: the index).  stride and every offset are multiples of 4.
+struct HostRecords {
+    char *base;
+    uint32_t stride, id_bytes;
+    int32_t off_id, off_type, off_mass, off_position, off_velocity, off_colour;
+};
+constexpr uint32_t kMaxRecordStride = 128;  // bytes; the upload stages a tile of records in shared memory
+void launch_pack_records(const HostRecords &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
+                         uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st);
+// the HostParticlesOut of a HostRecords (stride set)
+HostParticlesOut record_fields(const HostRecords &r, bool motion, bool fixed);
+
+// Cell queries against the grid of a batch's last step (query.cu): for each point,
+// the fluid particles in its grid cell and their mean ARGB colour, before the
+// step's colour diffusion (include/fluid/oclsph.hpp:770-791).
+void launch_queries(const SceneDev *scenes, uint32_t scene, float h, const uint2 *cells, const int32_t *type_sorted,
+                    const uint32_t *order, const uint32_t *colour_prev, const fgb_query *q, uint32_t nq,
+                    uint32_t *count, uint32_t *argb, cudaStream_t st);
 void launch_pack_from_host(const HostParticlesIn &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
                            uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st);
 void launch_unpack_to_host(const HostParticlesOut &out, uint64_t n, const float4 *x, const float4 *v,

@@ -150,18 +150,90 @@ __global__ void __launch_bounds__(kTile) k_unpack_static(HostParticlesOut out, u
                                                         const uint32_t *__restrict__ col,
                                                         const uint32_t *__restrict__ slot,
                                                         const uint64_t *__restrict__ ids) {
+    const uint64_t rs = out.stride;  // 0: packed arrays, else record i's fields i * stride further
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        if (out.mass) out.mass[i] = ps_grid[i].w;
-        if (out.type) out.type[i] = type[i];
-        if (out.colour) out.colour[i] = col[i];
+        if (out.mass) *(rs ? (float *)((char *)out.mass + i * rs) : out.mass + i) = ps_grid[i].w;
+        if (out.type) *(rs ? (int32_t *)((char *)out.type + i * rs) : out.type + i) = type[i];
+        if (out.colour) *(rs ? (uint32_t *)((char *)out.colour + i * rs) : out.colour + i) = col[i];
         if (out.id) {
             const uint32_t sl = slot[i];
-            out.id[i] = sl < n ? ids[sl] : sl;
+            const uint64_t id = sl < n ? ids[sl] : sl;
+            if (!rs) {
+                out.id[i] = id;
+            } else {  // records: 4-byte stores (a record's fields are 4-byte aligned)
+                uint32_t *q = (uint32_t *)((char *)out.id + i * rs);
+                q[0] = (uint32_t)id;
+                if (out.id_bytes == 8) q[1] = (uint32_t)(id >> 32);
+            }
         }
     }
 }
 
+// An upload from the caller's array of records: each CTA stages its tile of records
+// in shared memory as 4-byte words read in order (every warp access a contiguous run
+// of the host array), then each thread takes its particle's fields from there.
+__global__ void __launch_bounds__(kTile) k_pack_records(HostRecords in, uint64_t n, float4 *__restrict__ x,
+                                                       float4 *__restrict__ v, int32_t *__restrict__ type,
+                                                       uint32_t *__restrict__ col, uint32_t *__restrict__ slot,
+                                                       uint64_t *__restrict__ ids, uint32_t *__restrict__ obstacles) {
+    __shared__ uint32_t sw[kTile * (kMaxRecordStride / 4)];
+    const unsigned t = threadIdx.x;
+    const uint32_t words = in.stride / 4;
+    uint32_t obst = 0;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTile; base < n; base += (uint64_t)gridDim.x * kTile) {
+        const uint32_t m = (uint32_t)(n - base < kTile ? n - base : kTile);
+        const uint32_t *src = (const uint32_t *)(in.base + base * in.stride);
+        for (uint32_t j = t; j < m * words; j += kTile) sw[j] = src[j];
+        __syncthreads();
+        if (t < m) {
+            const uint64_t i = base + t;
+            const uint32_t *r = sw + t * words;
+            auto f32 = [&](int32_t off, int k) { return __uint_as_float(r[off / 4 + k]); };
+            const float mass = in.off_mass >= 0 ? f32(in.off_mass, 0) : 0.f;
+            const int32_t ty = in.off_type >= 0 ? (int32_t)r[in.off_type / 4] : FGB_TYPE_FLUID;
+            x[i] = make_float4(f32(in.off_position, 0), f32(in.off_position, 1), f32(in.off_position, 2), mass);
+            v[i] = make_float4(f32(in.off_velocity, 0), f32(in.off_velocity, 1), f32(in.off_velocity, 2), 0.f);
+            type[i] = ty;
+            col[i] = in.off_colour >= 0 ? r[in.off_colour / 4] : 0xffffffffu;
+            slot[i] = (uint32_t)i;
+            uint64_t id = i;
+            if (in.off_id >= 0) {
+                id = r[in.off_id / 4];
+                if (in.id_bytes == 8) id |= (uint64_t)r[in.off_id / 4 + 1] << 32;
+            }
+            ids[i] = id;
+            obst += ty == FGB_TYPE_OBSTACLE;
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o; o >>= 1) obst += __shfl_xor_sync(0xffffffffu, obst, o);
+    if ((t & 31) == 0 && obst) atomicAdd(obstacles, obst);
+}
+
 }  // namespace
+
+void launch_pack_records(const HostRecords &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
+                         uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st) {
+    if (n) k_pack_records<<<grid_of(n), kTile, 0, st>>>(in, n, x, v, type, col, slot, ids, obstacles);
+}
+
+HostParticlesOut record_fields(const HostRecords &r, bool motion, bool fixed) {
+    auto at = [&](int32_t off) { return off >= 0 ? (void *)(r.base + off) : nullptr; };
+    HostParticlesOut o{};
+    if (motion) {
+        o.position = (float *)at(r.off_position);
+        o.velocity = (float *)at(r.off_velocity);
+    }
+    if (fixed) {
+        o.mass = (float *)at(r.off_mass);
+        o.type = (int32_t *)at(r.off_type);
+        o.colour = (uint32_t *)at(r.off_colour);
+        o.id = (uint64_t *)at(r.off_id);
+    }
+    o.stride = r.stride;
+    o.id_bytes = r.id_bytes;
+    return o;
+}
 
 void launch_unpack_static(const HostParticlesOut &out, uint64_t n, const float4 *ps_grid, const int32_t *type,
                           const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st) {

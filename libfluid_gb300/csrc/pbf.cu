@@ -24,6 +24,13 @@ namespace {
 
 constexpr int kRef = FGB_PROFILE_REF;
 
+// Squared distance of a pair in the baseline profile's gathers: two fused
+// multiply-adds, as the oracle's baseline restatement computes it (the ref profile
+// keeps the reference's sum of three products).
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+}
+
 // Predicted position of one particle in solver units (oclsph.hpp:297-323).
 __device__ __forceinline__ float3 predict(const Phys &ph, const SceneDev &S, const WellDev *wells, int32_t type,
                                           float4 x, float4 v) {
@@ -151,26 +158,35 @@ struct GatherArgs {
     float list_r2, skin;
     const float4 *ps_grid;
     float *disp;
-    uint32_t *cellmax;
+    float *dstep;
+    uint2 *cellmax;
     uint8_t *valid;
     uint32_t *hlist;
     uint16_t *hcount;
     uint32_t hcap;
     uint8_t *near;  // null: no near rows
+    float *slack;
     float near_r2, near_skin;
     uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
+    uint32_t *near_stats;  // null, or warps of checked passes on near rows [0] / filtering [1]
+    // shared-memory halo per CTA of kHaloThreads particles (null: every CTA reads
+    // global memory); the build pass writes them, the later passes of the step read them
+    struct HaloHdr *halo_hdr;
+    uint2 *halo_box;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
 
-__device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t *__restrict__ cellmax,
-                                               uint32_t key, uint32_t mbits) {
+// The largest displacements over the 27 cells around a's cell: {since the grid was
+// built, in the last delta pass}.
+__device__ __forceinline__ float2 max_cell_disp(const SceneDev &S, const uint2 *__restrict__ cellmax,
+                                                uint32_t key, uint32_t mbits) {
     const uint32_t m = morton_of(key, mbits);
     const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
     const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
-    const uint32_t *tbl = cellmax + S.table_base;
+    const uint2 *tbl = cellmax + S.table_base;
     const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
-    uint32_t best = 0;  // non-negative floats order like their bit patterns
+    uint32_t best = 0, best_step = 0;  // non-negative floats order like their bit patterns
     for (int dz = -1; dz <= 1; ++dz) {
         const int z = cz + dz;
         if (z < 0 || z > ez) continue;
@@ -178,128 +194,209 @@ __device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t
             const int y = cy + dy;
             if (y < 0 || y > ey) continue;
             const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-            for (int x = x0; x <= x1; ++x) best = max(best, __ldg(&tbl[spread10((uint32_t)x) | yz]));
+            for (int x = x0; x <= x1; ++x) {
+                const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
+                best = max(best, c.x);
+                best_step = max(best_step, c.y);
+            }
         }
     }
-    return __uint_as_float(best);
+    return make_float2(__uint_as_float(best), __uint_as_float(best_step));
 }
 
 // Whether particle a may use its list for the current positions.
-// mcd: the 27 cells' maximum displacement when the caller already has it, else < 0.
+// mcd: the 27 cells' maximum displacement since the grid was built when the caller
+// already has it, else < 0 (then computed here and returned through it).
 template <int MODE>
 __device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
-                                         float mcd = -1.f) {
+                                         float &mcd) {
     if (A.cap == 0 || MODE == kBuild) return false;
     const uint16_t c = A.ncount[a];
     if (c == kListOverflow) return false;
     if (MODE == kFresh) return true;
     if (MODE == kStored) return A.valid[a] != 0;
-    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits).x;
     const bool ok = A.disp[a] + mcd <= A.skin;
     A.valid[a] = ok ? 1 : 0;
     return ok;
 }
 
-// Visit the candidates of particle a in walk order as f(b, p_b).  Loads run four
-// candidates ahead of the arithmetic (indices, then positions), so the dependent
-// index -> position -> math chain does not serialise on memory latency.
+// ------------------------------------------------------------------- halo
+//
+// Shared-memory halo.  The gathers' neighbour reads are scattered: each lane reads its
+// own neighbours' 16-byte records, ~20 distinct sectors a warp load, and the L1 data
+// pipe (shared with shared memory) saturates on them.  In halo mode a CTA of
+// kHaloThreads consecutive sorted particles first copies into shared memory, cell run
+// after cell run, the per-particle data its pass reads of neighbours (p* and the
+// pass's second array) for every cell of its box: the bounding box of its particles'
+// cells grown by one cell on every side and cut to the grid.  All 27 neighbour cells
+// of every particle of the CTA lie in the box.  The rows of the step (Verlet, hit and
+// near rows) then hold slots of that copy instead of particle indices, and a walk
+// finds a neighbour cell's slots through the box table.  The step's list-build pass
+// builds each CTA's box and table and writes them out; every later pass of the step
+// runs the same CTAs over the same particles and reads them back.  A CTA whose
+// particles span two scenes, whose box exceeds kHaloBox cells or whose cells hold
+// more than kHaloCap particles reads global memory instead.  Walks and rows keep their
+// order, so every sum is the same either way.
+constexpr uint32_t kHaloThreads = 256;
+constexpr uint32_t kHaloCap = 2048;  // particles a CTA stages
+constexpr uint32_t kHaloBox = 512;   // cells of a CTA's box
+
+struct HaloHdr {
+    int32_t ok;          // 1: the CTA reads its halo from shared memory
+    int32_t x0, y0, z0;  // box origin, cells
+    int32_t bx, by, bz;  // box extent, cells
+    uint32_t vol, parts; // cells in the box, particles staged
+};
+
+// Box table entry: {first particle of the cell, slot of its first particle << 16 |
+// particles in the cell}.
+__device__ __forceinline__ uint32_t box_slot(uint2 e) { return e.y >> 16; }
+__device__ __forceinline__ uint32_t box_count(uint2 e) { return e.y & 0xffffu; }
+
+// Copy the halo's runs into shared memory: one warp per box cell, its particles'
+// records read as one contiguous run.  sex / sty may be null.
+template <class T>
+__device__ __forceinline__ void halo_copy(const uint2 *box, uint32_t vol, const float4 *__restrict__ ps,
+                                          float4 *sps, const T *__restrict__ ex, T *sex,
+                                          const int32_t *__restrict__ type, uint8_t *sty) {
+    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t i = w; i < vol; i += nw) {
+        const uint2 e = box[i];
+        const uint32_t start = e.x, off = box_slot(e), cnt = box_count(e);
+        for (uint32_t k = lane; k < cnt; k += 32) {
+            sps[off + k] = __ldg(&ps[start + k]);
+            if (sex) sex[off + k] = __ldg(&ex[start + k]);
+            if (sty) sty[off + k] = (uint8_t)__ldg(&type[start + k]);
+        }
+    }
+}
+
+// The list-build pass: this CTA's box, its table (counts, then slots by an exclusive
+// scan in box order) and the staged p*.  Every thread of the CTA calls it; returns
+// whether the CTA runs in halo mode.
+__device__ bool halo_build(const GatherArgs &A, const float4 *__restrict__ ps, HaloHdr &h, uint2 *box,
+                           float4 *sps) {
+    __shared__ int s_lo[3], s_hi[3];
+    __shared__ uint32_t s_scene[2], s_warp[kHaloThreads / 32];
+    const uint32_t tid = threadIdx.x, a = blockIdx.x * blockDim.x + tid;
+    if (tid == 0) {
+        for (int d = 0; d < 3; ++d) s_lo[d] = 0x7fffffff, s_hi[d] = -1;
+        s_scene[0] = 0xffffffffu, s_scene[1] = 0u;
+    }
+    __syncthreads();
+    if (a < A.n) {
+        const uint32_t key = A.keys[a], m = morton_of(key, A.mbits), sc = scene_of(key, A.mbits);
+        const int c[3] = {(int)compact10(m), (int)compact10(m >> 1), (int)compact10(m >> 2)};
+        for (int d = 0; d < 3; ++d) atomicMin(&s_lo[d], c[d]), atomicMax(&s_hi[d], c[d]);
+        atomicMin(&s_scene[0], sc);
+        atomicMax(&s_scene[1], sc);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        HaloHdr t{};
+        if (s_scene[0] == s_scene[1]) {
+            const SceneDev &S = A.scenes[s_scene[0]];
+            int lo[3], hi[3];
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = s_lo[d] > 0 ? s_lo[d] - 1 : 0;
+                hi[d] = s_hi[d] < (int)S.ext[d] ? s_hi[d] + 1 : (int)S.ext[d];
+            }
+            t.x0 = lo[0], t.y0 = lo[1], t.z0 = lo[2];
+            t.bx = hi[0] - lo[0] + 1, t.by = hi[1] - lo[1] + 1, t.bz = hi[2] - lo[2] + 1;
+            const uint64_t vol = (uint64_t)t.bx * (uint64_t)t.by * (uint64_t)t.bz;
+            t.ok = vol <= kHaloBox;
+            t.vol = t.ok ? (uint32_t)vol : 0u;
+        }
+        h = t;
+    }
+    __syncthreads();
+    if (h.ok) {
+        const SceneDev &S = A.scenes[s_scene[0]];
+        const uint2 *tbl = A.cells + S.table_base;
+        for (uint32_t i = tid; i < h.vol; i += blockDim.x) {
+            const uint32_t x = (uint32_t)h.x0 + i % (uint32_t)h.bx;
+            const uint32_t y = (uint32_t)h.y0 + (i / (uint32_t)h.bx) % (uint32_t)h.by;
+            const uint32_t z = (uint32_t)h.z0 + i / ((uint32_t)h.bx * (uint32_t)h.by);
+            const uint2 c = __ldg(&tbl[morton3(x, y, z)]);
+            box[i] = make_uint2(c.x, c.y > c.x ? c.y - c.x : 0u);
+        }
+        __syncthreads();
+        // exclusive scan of the counts in box order: two entries a thread
+        const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
+        const uint32_t c0 = i0 < h.vol ? box[i0].y : 0u, c1 = i1 < h.vol ? box[i1].y : 0u;
+        uint32_t x = c0 + c1;
+        const uint32_t lane = tid & 31u, w = tid >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_warp[w] = x;
+        __syncthreads();
+        uint32_t base = 0, total = 0;
+        for (uint32_t k = 0; k < blockDim.x / 32; ++k) {
+            if (k < w) base += s_warp[k];
+            total += s_warp[k];
+        }
+        const uint32_t ex0 = base + x - (c0 + c1);
+        // counts stay below 2^16 and slots below kHaloCap where the CTA stages
+        if (i0 < h.vol) box[i0].y = (min(ex0, 0xffffu) << 16) | min(c0, 0xffffu);
+        if (i1 < h.vol) box[i1].y = (min(ex0 + c0, 0xffffu) << 16) | min(c1, 0xffffu);
+        __syncthreads();
+        if (tid == 0) {
+            h.parts = total;
+            if (total > kHaloCap) h.ok = 0;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) A.halo_hdr[blockIdx.x] = h;
+    if (!h.ok) return false;
+    uint2 *gbox = A.halo_box + (size_t)blockIdx.x * kHaloBox;
+    for (uint32_t i = tid; i < h.vol; i += blockDim.x) gbox[i] = box[i];
+    halo_copy<float>(box, h.vol, ps, sps, nullptr, nullptr, nullptr, nullptr);
+    __syncthreads();
+    return true;
+}
+
+// A later pass of the step: this CTA's box and table as the build pass left them, and
+// the pass's arrays staged.  Every thread of the CTA calls it.
+template <class T>
+__device__ bool halo_load(const GatherArgs &A, HaloHdr &h, uint2 *box, float4 *sps, const float4 *__restrict__ ps,
+                          T *sex, const T *__restrict__ ex, uint8_t *sty) {
+    if (threadIdx.x == 0) h = A.halo_hdr[blockIdx.x];
+    __syncthreads();
+    if (!h.ok) return false;
+    const uint2 *gbox = A.halo_box + (size_t)blockIdx.x * kHaloBox;
+    for (uint32_t i = threadIdx.x; i < h.vol; i += blockDim.x) box[i] = gbox[i];
+    __syncthreads();
+    halo_copy<T>(box, h.vol, ps, sps, ex, sex, A.type, sty);
+    __syncthreads();
+    return true;
+}
+
+// Where a gather finds its neighbours' data.  GlobalSpace: the batch arrays by sorted
+// particle index, walks through the cell table.  HaloSpace: the CTA's shared-memory
+// copy by slot, walks through the box table.  pos(b): p* of candidate b; x(b): the
+// pass's second array; fluid(b): whether b is not an obstacle.
 constexpr int kPrefetch = 4;
 
-template <class F>
-__device__ __forceinline__ void visit_range(uint32_t lo, uint32_t hi, const float4 *__restrict__ ps, F &f) {
-    uint32_t b = lo;
-    for (; b + kPrefetch <= hi; b += kPrefetch) {
-        float4 p[kPrefetch];
-#pragma unroll
-        for (int k = 0; k < kPrefetch; ++k) p[k] = __ldg(&ps[b + k]);
-#pragma unroll
-        for (int k = 0; k < kPrefetch; ++k) f(b + k, p[k]);
-    }
-    for (; b < hi; ++b) f(b, __ldg(&ps[b]));
-}
-
-// Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
-// a multiple of 4) as f(b, p_b); indices arrive four at a time as one 16-byte load,
-// and the four positions are loaded before any arithmetic.
-// kSameKernel: the row was written earlier in this kernel, so it is read through L2
-// (ld.global.cg) rather than the read-only path.
-template <bool kSameKernel = false, class F>
-__device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
-                                        const float4 *__restrict__ ps, F &f) {
-    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
-    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
-    // software pipeline: the next index vector is in flight while the current four
-    // candidates are loaded and processed (rows usually stream from HBM)
-    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
-    uint32_t j = 0;
-    for (; j + 4 <= c; j += 4) {
-        const uint4 b = next;
-        if (j + 4 < c) next = load(j + 4);
-        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
-        f(b.x, p0);
-        f(b.y, p1);
-        f(b.z, p2);
-        f(b.w, p3);
-    }
-    if (j < c) {
-        const uint4 b = next;
-        const uint32_t rest = c - j;
-        const float4 p0 = __ldg(&ps[b.x]);
-        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
-        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
-        f(b.x, p0);
-        if (rest > 1) f(b.y, p1);
-        if (rest > 2) f(b.z, p2);
-    }
-}
-
-// for_row with a second per-candidate value gathered beside each position (the
-// delta pass's lambda_b, the vorticity passes' v_b and |omega_b|): the four values
-// load together with the four positions, ahead of the arithmetic, instead of inside
-// it after the range test.  f(b, p_b, get) with get() returning the value.
-template <bool kSameKernel = false, class T, class F>
-__device__ __forceinline__ void for_row_x(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
-                                          const float4 *__restrict__ ps, const T *__restrict__ ex, F &f) {
-    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
-    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
-    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
-    uint32_t j = 0;
-    for (; j + 4 <= c; j += 4) {
-        const uint4 b = next;
-        if (j + 4 < c) next = load(j + 4);
-        const float4 p0 = __ldg(&ps[b.x]), p1 = __ldg(&ps[b.y]), p2 = __ldg(&ps[b.z]), p3 = __ldg(&ps[b.w]);
-        const T e0 = __ldg(&ex[b.x]), e1 = __ldg(&ex[b.y]), e2 = __ldg(&ex[b.z]), e3 = __ldg(&ex[b.w]);
-        f(b.x, p0, [&] { return e0; });
-        f(b.y, p1, [&] { return e1; });
-        f(b.z, p2, [&] { return e2; });
-        f(b.w, p3, [&] { return e3; });
-    }
-    if (j < c) {
-        const uint4 b = next;
-        const uint32_t rest = c - j;
-        const float4 p0 = __ldg(&ps[b.x]);
-        const float4 p1 = rest > 1 ? __ldg(&ps[b.y]) : p0;
-        const float4 p2 = rest > 2 ? __ldg(&ps[b.z]) : p0;
-        const T e0 = __ldg(&ex[b.x]);
-        const T e1 = rest > 1 ? __ldg(&ex[b.y]) : e0;
-        const T e2 = rest > 2 ? __ldg(&ex[b.z]) : e0;
-        f(b.x, p0, [&] { return e0; });
-        if (rest > 1) f(b.y, p1, [&] { return e1; });
-        if (rest > 2) f(b.z, p2, [&] { return e2; });
-    }
-}
-
-template <class F>
-__device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
-                                               bool list, const float4 *__restrict__ ps, F &&f) {
-    if (list) {
-        for_row(A.nlist, A.cap, a, A.ncount[a], ps, f);
-    } else {
+template <class T>
+struct GlobalSpace {
+    const float4 *ps;
+    const T *ex;
+    const int32_t *type;
+    __device__ __forceinline__ float4 pos(uint32_t b) const { return __ldg(&ps[b]); }
+    __device__ __forceinline__ T x(uint32_t b) const { return __ldg(&ex[b]); }
+    __device__ __forceinline__ bool fluid(uint32_t b) const { return __ldg(&type[b]) != FGB_TYPE_OBSTACLE; }
+    // Visit the particles of the 27 cells in walk order as f(b, p_b); loads run four
+    // candidates ahead of the arithmetic.
+    template <class F>
+    __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f) const {
         const uint32_t m = morton_of(key, A.mbits);
         const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
-        const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+        const int ex_ = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
         const uint2 *tbl = A.cells + S.table_base;
-        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex_ ? cx + 1 : ex_;
         for (int dz = -1; dz <= 1; ++dz) {
             const int z = cz + dz;
             if (z < 0 || z > ez) continue;
@@ -309,11 +406,133 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
                 const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
                 for (int x = x0; x <= x1; ++x) {
                     const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                    visit_range(c.x, c.y, ps, f);
+                    visit(c.x, c.y, f);
                 }
             }
         }
     }
+    template <class F>
+    __device__ __forceinline__ void visit(uint32_t lo, uint32_t hi, F &f) const {
+        uint32_t b = lo;
+        for (; b + kPrefetch <= hi; b += kPrefetch) {
+            float4 p[kPrefetch];
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) p[k] = pos(b + k);
+#pragma unroll
+            for (int k = 0; k < kPrefetch; ++k) f(b + k, p[k]);
+        }
+        for (; b < hi; ++b) f(b, pos(b));
+    }
+};
+
+template <class T>
+struct HaloSpace {
+    const float4 *ps;   // shared memory, by slot
+    const T *ex;        // shared memory, by slot
+    const uint8_t *type;
+    const uint2 *box;
+    HaloHdr h;
+    __device__ __forceinline__ float4 pos(uint32_t b) const { return ps[b]; }
+    __device__ __forceinline__ T x(uint32_t b) const { return ex[b]; }
+    __device__ __forceinline__ bool fluid(uint32_t b) const { return type[b] != FGB_TYPE_OBSTACLE; }
+    template <class F>
+    __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f) const {
+        const uint32_t m = morton_of(key, A.mbits);
+        const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
+        const int ex_ = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex_ ? cx + 1 : ex_;
+        for (int dz = -1; dz <= 1; ++dz) {
+            const int z = cz + dz;
+            if (z < 0 || z > ez) continue;
+            for (int dy = -1; dy <= 1; ++dy) {
+                const int y = cy + dy;
+                if (y < 0 || y > ey) continue;
+                const int row = h.bx * ((y - h.y0) + h.by * (z - h.z0)) - h.x0;
+                for (int x = x0; x <= x1; ++x) {
+                    const uint2 e = box[row + x];
+                    const uint32_t lo = box_slot(e);
+                    for (uint32_t b = lo; b < lo + box_count(e); ++b) f(b, ps[b]);
+                }
+            }
+        }
+    }
+};
+
+// Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
+// a multiple of 4) as f(b, p_b); indices arrive four at a time as one 16-byte load,
+// and the four positions are loaded before any arithmetic.
+// kSameKernel: the row was written earlier in this kernel, so it is read through L2
+// (ld.global.cg) rather than the read-only path.
+template <bool kSameKernel = false, class Sp, class F>
+__device__ __forceinline__ void for_row(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
+                                        const Sp &sp, F &f) {
+    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
+    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
+    // software pipeline: the next index vector is in flight while the current four
+    // candidates are loaded and processed (rows usually stream from HBM)
+    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
+    uint32_t j = 0;
+    for (; j + 4 <= c; j += 4) {
+        const uint4 b = next;
+        if (j + 4 < c) next = load(j + 4);
+        const float4 p0 = sp.pos(b.x), p1 = sp.pos(b.y), p2 = sp.pos(b.z), p3 = sp.pos(b.w);
+        f(b.x, p0);
+        f(b.y, p1);
+        f(b.z, p2);
+        f(b.w, p3);
+    }
+    if (j < c) {
+        const uint4 b = next;
+        const uint32_t rest = c - j;
+        const float4 p0 = sp.pos(b.x);
+        const float4 p1 = rest > 1 ? sp.pos(b.y) : p0;
+        const float4 p2 = rest > 2 ? sp.pos(b.z) : p0;
+        f(b.x, p0);
+        if (rest > 1) f(b.y, p1);
+        if (rest > 2) f(b.z, p2);
+    }
+}
+
+// for_row with the pass's second array gathered beside each position (the delta
+// pass's lambda_b, the vorticity passes' v_b and omega_b): the four values load with
+// the four positions, ahead of the arithmetic.  f(b, p_b, get) with get() the value.
+template <bool kSameKernel = false, class Sp, class F>
+__device__ __forceinline__ void for_row_x(const uint32_t *__restrict__ base, uint32_t cap, uint32_t a, uint32_t c,
+                                          const Sp &sp, F &f) {
+    const uint4 *row = reinterpret_cast<const uint4 *>(base + (size_t)a * cap);
+    auto load = [&](uint32_t j) { return kSameKernel ? __ldcg(row + (j >> 2)) : __ldg(row + (j >> 2)); };
+    uint4 next = c ? load(0) : make_uint4(0, 0, 0, 0);
+    uint32_t j = 0;
+    for (; j + 4 <= c; j += 4) {
+        const uint4 b = next;
+        if (j + 4 < c) next = load(j + 4);
+        const float4 p0 = sp.pos(b.x), p1 = sp.pos(b.y), p2 = sp.pos(b.z), p3 = sp.pos(b.w);
+        const auto e0 = sp.x(b.x), e1 = sp.x(b.y), e2 = sp.x(b.z), e3 = sp.x(b.w);
+        f(b.x, p0, [&] { return e0; });
+        f(b.y, p1, [&] { return e1; });
+        f(b.z, p2, [&] { return e2; });
+        f(b.w, p3, [&] { return e3; });
+    }
+    if (j < c) {
+        const uint4 b = next;
+        const uint32_t rest = c - j;
+        const float4 p0 = sp.pos(b.x);
+        const float4 p1 = rest > 1 ? sp.pos(b.y) : p0;
+        const float4 p2 = rest > 2 ? sp.pos(b.z) : p0;
+        const auto e0 = sp.x(b.x);
+        const auto e1 = rest > 1 ? sp.x(b.y) : e0;
+        const auto e2 = rest > 2 ? sp.x(b.z) : e0;
+        f(b.x, p0, [&] { return e0; });
+        if (rest > 1) f(b.y, p1, [&] { return e1; });
+        if (rest > 2) f(b.z, p2, [&] { return e2; });
+    }
+}
+
+template <class Sp, class F>
+__device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
+                                               bool list, const Sp &sp, F &&f) {
+    if (list) for_row(A.nlist, A.cap, a, A.ncount[a], sp, f);
+    else sp.walk(A, S, key, f);
 }
 
 // Hit lists.  A lambda pass and the delta pass after it read the same p*, so they
@@ -327,16 +546,22 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 // walk.  A row that overflows (count > hcap) sends its passes back to the candidates.
 // Rows are particle-major like the Verlet lists.
 //
-// Near rows.  The build pass (the step's first lambda pass) keeps in the hit row
-// every candidate within h + near_skin of the grid positions rather than within h,
-// and marks the row (near[a]).  By the same bound as the Verlet lists, that row still
-// holds every neighbour within h while disp_a + max disp_b <= near_skin, so a later
-// lambda pass for which the bound holds runs its arithmetic straight over the row,
-// without the range-filter phase, and leaves the row for the delta pass after it.
-// The extra entries (~15% at 0.05 h) fail the passes' own range tests, so the sums
-// are unchanged.  A pass for which the bound fails (for any lane of the warp) filters
-// as before and clears the mark: the row it writes holds the hits of that pass's
-// positions only.
+// Near rows.  A lambda pass that filters its candidates keeps in the hit row every
+// candidate within h + near_skin of that pass's positions rather than within h, and
+// marks the row (near[a]) with slack[a] = 0.  The row still holds every neighbour
+// within h while the distance a and any candidate have moved since, added up over the
+// passes in between, stays within near_skin: each delta pass records the distance
+// every particle moved (dstep) and its per-cell maximum, and each later pass adds
+// dstep_a + the largest dstep of the 27 cells to slack[a].  A later lambda pass whose
+// warp's rows all hold runs its arithmetic straight over them, without the
+// range-filter phase, and leaves them for the delta pass after it; the vorticity pass
+// likewise.  The extra entries (~15% at 0.05 h) fail the passes' own range tests, so
+// the sums are unchanged.  A warp for which the bound fails on any lane filters
+// again and writes fresh near rows at its current positions -- from a walk, or from
+// a Verlet list whose own bound leaves near_skin of its skin (else the row holds that
+// pass's hits within h and loses the mark).  Bounding the motion per pass rather than
+// since the grid was built keeps rows usable deep into a violent flow, where some
+// particle in nearly every neighbourhood has moved far since the step began.
 struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
@@ -371,20 +596,28 @@ __device__ __forceinline__ void close_hits_empty(const GatherArgs &A, uint32_t a
     if (A.hcap) A.hcount[a] = 0;
 }
 
+// One count per warp of a checked pass: whether it ran on its near rows.
+__device__ __forceinline__ void count_near(const GatherArgs &A, bool on_rows) {
+    if (!A.near_stats) return;
+    const unsigned m = __activemask();
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.near_stats[on_rows ? 0 : 1], 1u);
+}
+
 __device__ __forceinline__ bool have_hits(const GatherArgs &A, uint32_t a) {
     return A.hcap != 0 && A.hcount[a] != kListOverflow;
 }
 
-template <class F>
-__device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const float4 *__restrict__ ps, F &&f) {
-    for_row(A.hlist, A.hcap, a, A.hcount[a], ps, f);
+template <class Sp, class F>
+__device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const Sp &sp, F &&f) {
+    for_row(A.hlist, A.hcap, a, A.hcount[a], sp, f);
 }
 
 // The step's Verlet lists on their own: each particle walks its 27 cells and keeps, in
 // walk order, every candidate within h + skin.  The first lambda pass then filters the
 // fresh lists (near rows) instead of walking, so the walk carries one row writer and
 // no kernel arithmetic.
-__global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 *__restrict__ ps) {
+template <class Sp>
+__device__ __forceinline__ void build_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
@@ -397,7 +630,7 @@ __global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 
     RowWriter built(A.nlist, A.cap, a);
     // membership only (the passes re-test every entry exactly): a contracted r^2,
     // within ~2e-7 of the sum of squares, against a radius rounded up by 1e-5
-    for_candidates(A, S, a, key, false, ps, [&](uint32_t b, const float4 &pb) {
+    for_candidates(A, S, a, key, false, sp, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
     });
@@ -409,9 +642,28 @@ __global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 
     }
 }
 
-template <int PROFILE, int MODE>
-__global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
-                                                float *__restrict__ lambda, float *__restrict__ density) {
+// Shared memory of the halo: the box table, then the staged p*, then the pass's
+// second array (T) and the types, as the pass needs them.
+template <class T, bool kTypes>
+constexpr size_t halo_smem_bytes() {
+    return kHaloBox * sizeof(uint2) + kHaloCap * sizeof(float4) + (sizeof(T) > 1 ? kHaloCap * sizeof(T) : 0) +
+           (kTypes ? kHaloCap : 0);
+}
+
+__global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 *__restrict__ ps) {
+    extern __shared__ uint4 halo_smem[];
+    __shared__ HaloHdr h;
+    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
+    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
+    if (A.halo_hdr && halo_build(A, ps, h, box, sps))
+        build_body(A, HaloSpace<char>{sps, nullptr, nullptr, box, h}, ps);
+    else
+        build_body(A, GlobalSpace<char>{ps, nullptr, A.type}, ps);
+}
+
+template <int PROFILE, int MODE, class Sp>
+__device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+                                            float *__restrict__ lambda, float *__restrict__ density) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
@@ -428,8 +680,8 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     float rho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, g2 = 0.f;
     auto body = [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
+            const float r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 <= ph.hh_le)) return;  // sqrtf(r2) > h: no contribution
             const float r = sqrtf(r2);
             if (r <= ph.h) {
@@ -444,17 +696,18 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                 }
             }
         } else {
-            if (r2 <= ph.hh) {
-                const float t = ph.hh - r2;
+            const float q2 = dist2(dx, dy, dz);
+            if (q2 <= ph.hh) {
+                const float t = ph.hh - q2;
                 rho = __fmaf_rn(pb.w, t * t * t, rho);
-                const float r = sqrtf(r2);
+                const float r = sqrtf(q2);
                 if (r >= kKernelEpsilon) {
                     const float hr = ph.h - r;
                     const float sc = pb.w * ((hr * hr) / r);
                     gx = __fmaf_rn(sc, dx, gx);
                     gy = __fmaf_rn(sc, dy, gy);
                     gz = __fmaf_rn(sc, dz, gz);
-                    g2 = __fmaf_rn(sc * sc, r2, g2);
+                    g2 = __fmaf_rn(sc * sc, q2, g2);
                 }
             }
         }
@@ -466,13 +719,19 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     bool done = false;
     if (MODE == kCheck && A.near) {
         bool ok = false;
+        float slack = 0.f;
         if (A.near[a] && have_hits(A, a)) {
-            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
-            ok = A.disp[a] + mcd <= A.near_skin;
+            const float2 m = max_cell_disp(S, A.cellmax, key, A.mbits);
+            mcd = m.x;
+            slack = A.slack[a] + (A.dstep[a] + m.y);
+            ok = slack <= A.near_skin;
         }
         done = __all_sync(__activemask(), ok);
-        if (done) for_hits(A, a, ps, body);
-        else A.near[a] = 0;
+        count_near(A, done);
+        if (done) {
+            A.slack[a] = slack;
+            for_hits(A, a, sp, body);
+        }
     }
     if (!done) {
         bool list = use_list<MODE>(A, S, a, key, mcd);
@@ -483,16 +742,20 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
         // the choice per lane.
         if constexpr (MODE == kCheck && PROFILE == kRef) list = __all_sync(__activemask(), list);
         if (A.hcap == 0 && MODE != kBuild) {
-            for_candidates(A, S, a, key, list, ps, body);
+            for_candidates(A, S, a, key, list, sp, body);
         } else {
             // phase 1: range filter (and the Verlet list on the build pass)
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
-            const bool near_row = (MODE == kBuild || MODE == kFresh) && A.near;
+            // the row written here is a near row when its candidates hold every one
+            // within h + near_skin: a walk, a fresh list, or a checked list whose bound
+            // leaves near_skin of its skin
+            const bool near_row =
+                A.near && (MODE == kBuild || MODE == kFresh || !list || A.disp[a] + mcd <= A.skin - A.near_skin);
             // membership only (the arithmetic re-tests every entry exactly): a contracted
             // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
             const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
-            for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+            for_candidates(A, S, a, key, list, sp, [&](uint32_t b, const float4 &pb) {
                 const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
                 const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
                 if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
@@ -509,10 +772,13 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
                     if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
                 }
             }
-            if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
+            if (A.near) {
+                A.near[a] = near_row && A.hcap && hits.count <= A.hcap ? 1 : 0;
+                if (near_row) A.slack[a] = 0.f;
+            }
             // phase 2: the kernel arithmetic over the hits, in walk order
-            if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, ps, body);
-            else for_candidates(A, S, a, key, list, ps, body);
+            if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
+            else for_candidates(A, S, a, key, list, sp, body);
         }
     }
     float dens, lam;
@@ -531,6 +797,19 @@ __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__re
     }
     lambda[a] = lam;
     density[a] = dens;
+}
+
+template <int PROFILE, int MODE>
+__global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
+                                                float *__restrict__ lambda, float *__restrict__ density) {
+    extern __shared__ uint4 halo_smem[];
+    __shared__ HaloHdr h;
+    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
+    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
+    if (A.halo_hdr && halo_load<char>(A, h, box, sps, ps, nullptr, nullptr, nullptr))
+        lambda_body<PROFILE, MODE>(A, HaloSpace<char>{sps, nullptr, nullptr, box, h}, ps, lambda, density);
+    else
+        lambda_body<PROFILE, MODE>(A, GlobalSpace<char>{ps, nullptr, A.type}, ps, lambda, density);
 }
 
 __device__ __forceinline__ float corr_pow(float ratio, float n) {
@@ -607,30 +886,34 @@ __device__ __forceinline__ void collide_sphere(const SceneDev &S, float *pos) {
 __device__ __forceinline__ void store_host_motion(const HostParticlesOut *__restrict__ hout, uint32_t a,
                                                   const float4 &xa, const float4 &va) {
     if (!hout) return;
+    const uint32_t stride = hout->stride;  // 0: packed arrays, else the caller's records
     float *pp = hout->position, *pv = hout->velocity;
     if (pp) {
-        pp[3 * (size_t)a] = xa.x;
-        pp[3 * (size_t)a + 1] = xa.y;
-        pp[3 * (size_t)a + 2] = xa.z;
+        float *q = stride ? (float *)((char *)pp + (size_t)a * stride) : pp + 3 * (size_t)a;
+        q[0] = xa.x;
+        q[1] = xa.y;
+        q[2] = xa.z;
     }
     if (pv) {
-        pv[3 * (size_t)a] = va.x;
-        pv[3 * (size_t)a + 1] = va.y;
-        pv[3 * (size_t)a + 2] = va.z;
+        float *q = stride ? (float *)((char *)pv + (size_t)a * stride) : pv + 3 * (size_t)a;
+        q[0] = va.x;
+        q[1] = va.y;
+        q[2] = va.z;
     }
 }
 
-template <int PROFILE, int MODE>
-__global__ void __launch_bounds__(256)
-    k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
-            float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
-            const HostParticlesOut *__restrict__ hout) {
+template <int PROFILE, int MODE, class Sp>
+__device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps_in,
+                                           const float *__restrict__ lambda, float4 *__restrict__ ps_out,
+                                           float4 *__restrict__ x, float4 *__restrict__ v, int last,
+                                           const HostParticlesOut *__restrict__ hout) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     const float4 pa = ps_in[a];
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         ps_out[a] = pa;
         if (A.cap) A.disp[a] = 0.f;
+        if (A.dstep) A.dstep[a] = 0.f;
         if (PROFILE == kRef && last) store_host_motion(hout, a, x[a], v[a]);
         return;
     }
@@ -642,8 +925,8 @@ __global__ void __launch_bounds__(256)
     // lam_b() is lambda of b (gathered beside p_b on rows, loaded on demand on walks)
     auto body = [&](uint32_t b, const float4 &pb, auto lam_b) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
         if (PROFILE == kRef) {
+            const float r2 = dx * dx + dy * dy + dz * dz;
             if (!(r2 <= ph.hh_le)) return;  // sqrtf(r2) > h: no contribution
             const float r = sqrtf(r2);
             float w = 0.f;
@@ -661,11 +944,12 @@ __global__ void __launch_bounds__(256)
                 pz = __fmaf_rn(dz * sc, factor, pz);
             }
         } else {
-            if (r2 <= ph.hh) {
-                const float r = sqrtf(r2);
+            const float q2 = dist2(dx, dy, dz);
+            if (q2 <= ph.hh) {
+                const float r = sqrtf(q2);
                 if (r >= kKernelEpsilon) {
-                    const float t = ph.hh - r2;
-                    const float corr = -ph.corr_k * corr_pow((t * t * t) / ph.corr_wdq, ph.corr_n);
+                    const float t = ph.hh - q2;
+                    const float corr = -ph.corr_k * corr_pow((t * t * t) * ph.inv_corr_wdq, ph.corr_n);
                     const float hr = ph.h - r;
                     const float sc = pb.w * ((hr * hr) / r) * (la + lam_b() + corr);
                     px = __fmaf_rn(sc, dx, px);
@@ -676,10 +960,11 @@ __global__ void __launch_bounds__(256)
         }
     };
     if (have_hits(A, a)) {
-        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps_in, lambda, body);
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, body);
     } else {
-        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), ps_in, [&](uint32_t b, const float4 &pb) {
-            body(b, pb, [&] { return __ldg(&lambda[b]); });
+        float mcd = -1.f;
+        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key, mcd), sp, [&](uint32_t b, const float4 &pb) {
+            body(b, pb, [&] { return sp.x(b); });
         });
     }
     float world[3];
@@ -715,7 +1000,13 @@ __global__ void __launch_bounds__(256)
         const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);
         A.disp[a] = d;
-        atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
+        // and the distance moved by this pass, for the near rows' bound
+        const float sx = q[0] - pa.x, sy = q[1] - pa.y, sz = q[2] - pa.z;
+        const float ds = sqrtf(sx * sx + sy * sy + sz * sz);
+        if (A.dstep) A.dstep[a] = ds;
+        uint2 *cm = &A.cellmax[S.table_base + morton_of(key, A.mbits)];
+        atomicMax(&cm->x, __float_as_uint(d));
+        atomicMax(&cm->y, __float_as_uint(ds));
     }
     if (last) {
         const float4 xa = x[a];
@@ -738,6 +1029,24 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <int PROFILE, int MODE>
+__global__ void __launch_bounds__(256)
+    k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
+            float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
+            const HostParticlesOut *__restrict__ hout) {
+    extern __shared__ uint4 halo_smem[];
+    __shared__ HaloHdr h;
+    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
+    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
+    float *slam = reinterpret_cast<float *>(sps + kHaloCap);
+    if (A.halo_hdr && halo_load<float>(A, h, box, sps, ps_in, slam, lambda, nullptr))
+        delta_body<PROFILE, MODE>(A, HaloSpace<float>{sps, slam, nullptr, box, h}, ps_in, lambda, ps_out, x, v,
+                                  last, hout);
+    else
+        delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
+                                  hout);
+}
+
 __device__ __forceinline__ void cross3(const float *a, const float *b, float *o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
     o[1] = a[2] * b[0] - a[0] * b[2];
@@ -745,11 +1054,10 @@ __device__ __forceinline__ void cross3(const float *a, const float *b, float *o)
 }
 
 // Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
-
-// Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
-__global__ void __launch_bounds__(256)
-    k_vorticity_xsph(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ v,
-                     float4 *__restrict__ omega, float4 *__restrict__ vx) {
+template <class Sp>
+__device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+                                               const float4 *__restrict__ v, float4 *__restrict__ omega,
+                                               float4 *__restrict__ vx) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     const float4 va4 = v[a];
@@ -771,10 +1079,12 @@ __global__ void __launch_bounds__(256)
     if (A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
-            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
-            ok = A.disp[a] + mcd <= A.near_skin;
+            const float2 m = max_cell_disp(S, A.cellmax, key, A.mbits);
+            mcd = m.x;
+            ok = A.slack[a] + (A.dstep[a] + m.y) <= A.near_skin;
         }
         near = __all_sync(__activemask(), ok);
+        count_near(A, near);
         if (!near) A.near[a] = 0;
     }
     const bool list = near ? false : use_list<kCheck>(A, S, a, key, mcd);
@@ -783,9 +1093,9 @@ __global__ void __launch_bounds__(256)
     // fluid_known: b came from a filtered hit row, which holds fluid particles only;
     // vel_b() is v of b (gathered beside p_b on rows, loaded on demand on walks)
     auto body = [&](uint32_t b, const float4 &pb, auto vel_b, bool fluid_known) {
-        if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+        if (!fluid_known && S.obstacles && !sp.fluid(b)) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
-        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float r2 = dist2(d[0], d[1], d[2]);
         if (!(r2 <= ph.hh)) return;
         const float4 vb = vel_b();
         const float vab[3] = {vb.x - va[0], vb.y - va[1], vb.z - va[2]};
@@ -806,28 +1116,28 @@ __global__ void __launch_bounds__(256)
         }
     };
     auto any = [&](uint32_t b, const float4 &pb) {
-        body(b, pb, [&] { return __ldg(&v[b]); }, false);
+        body(b, pb, [&] { return sp.x(b); }, false);
     };
     if (near) {
         auto any_row = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, false); };
-        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps, v, any_row);
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, any_row);
     } else if (A.hcap == 0) {
-        for_candidates(A, S, a, key, list, ps, any);
+        for_candidates(A, S, a, key, list, sp, any);
     } else {
         // phase 1: fluid candidates within h; phase 2: the arithmetic over them
         HitWriter hits(A, a);
         const float hit_r2 = ph.hh * 1.000001f;  // membership only, as in the lambda filter
-        for_candidates(A, S, a, key, list, ps, [&](uint32_t b, const float4 &pb) {
+        for_candidates(A, S, a, key, list, sp, [&](uint32_t b, const float4 &pb) {
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
             const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-            if (r2 <= hit_r2 && (!S.obstacles || __ldg(&A.type[b]) != FGB_TYPE_OBSTACLE)) hits.add(b);
+            if (r2 <= hit_r2 && (!S.obstacles || sp.fluid(b))) hits.add(b);
         });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
             auto fluid = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, true); };
-            for_row_x<true>(A.hlist, A.hcap, a, hits.count, ps, v, fluid);
+            for_row_x<true>(A.hlist, A.hcap, a, hits.count, sp, fluid);
         } else {
-            for_candidates(A, S, a, key, list, ps, any);
+            for_candidates(A, S, a, key, list, sp, any);
         }
     }
     const float gs = ph.spikyf * ph.inv_rho0;
@@ -838,11 +1148,27 @@ __global__ void __launch_bounds__(256)
                         __fmaf_rn(ph.xsph_c, xs[2] * ws, va[2]), va4.w);
 }
 
-// Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
 __global__ void __launch_bounds__(256)
-    k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
-                      const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
-                      const HostParticlesOut *__restrict__ hout) {
+    k_vorticity_xsph(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ v,
+                     float4 *__restrict__ omega, float4 *__restrict__ vx) {
+    extern __shared__ uint4 halo_smem[];
+    __shared__ HaloHdr h;
+    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
+    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
+    float4 *sv = sps + kHaloCap;
+    uint8_t *sty = reinterpret_cast<uint8_t *>(sv + kHaloCap);
+    if (A.halo_hdr && halo_load<float4>(A, h, box, sps, ps, sv, v, sty))
+        vorticity_body(A, HaloSpace<float4>{sps, sv, sty, box, h}, ps, v, omega, vx);
+    else
+        vorticity_body(A, GlobalSpace<float4>{ps, v, A.type}, ps, v, omega, vx);
+}
+
+// Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
+template <class Sp>
+__device__ __forceinline__ void apply_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+                                           const float4 *__restrict__ omega, const float4 *__restrict__ vx,
+                                           float4 *__restrict__ v, float4 *__restrict__ x,
+                                           const HostParticlesOut *__restrict__ hout) {
     const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
@@ -858,9 +1184,9 @@ __global__ void __launch_bounds__(256)
     // fluid_known: b came from a filtered hit row, which holds fluid particles only;
     // om_b() is omega of b (gathered beside p_b on rows, loaded on demand on walks)
     auto body = [&](uint32_t b, const float4 &pb, auto om_b, bool fluid_known) {
-        if (!fluid_known && S.obstacles && __ldg(&A.type[b]) == FGB_TYPE_OBSTACLE) return;
+        if (!fluid_known && S.obstacles && !sp.fluid(b)) return;
         const float d[3] = {pa.x - pb.x, pa.y - pb.y, pa.z - pb.z};
-        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float r2 = dist2(d[0], d[1], d[2]);
         if (!(r2 <= ph.hh)) return;
         const float r = sqrtf(r2);
         if (!(r >= kKernelEpsilon)) return;
@@ -874,10 +1200,11 @@ __global__ void __launch_bounds__(256)
         // a near row (still marked) holds obstacles too; a filtered row fluid only
         const bool fluid_rows = !(A.near && A.near[a]);
         auto row = [&](uint32_t b, const float4 &pb, auto om_b) { body(b, pb, om_b, fluid_rows); };
-        for_row_x(A.hlist, A.hcap, a, A.hcount[a], ps, omega, row);
+        for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, row);
     } else {
-        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), ps, [&](uint32_t b, const float4 &pb) {
-            body(b, pb, [&] { return __ldg(&omega[b]); }, false);
+        float mcd = -1.f;
+        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key, mcd), sp, [&](uint32_t b, const float4 &pb) {
+            body(b, pb, [&] { return sp.x(b); }, false);
         });
     }
     const float gs = ph.spikyf * ph.inv_rho0;
@@ -901,6 +1228,22 @@ __global__ void __launch_bounds__(256)
     const float4 xn = make_float4(pa.x * S.scale, pa.y * S.scale, pa.z * S.scale, xa.w);
     x[a] = xn;
     store_host_motion(hout, a, xn, vn);
+}
+
+__global__ void __launch_bounds__(256)
+    k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
+                      const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
+                      const HostParticlesOut *__restrict__ hout) {
+    extern __shared__ uint4 halo_smem[];
+    __shared__ HaloHdr h;
+    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
+    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
+    float4 *som = sps + kHaloCap;
+    uint8_t *sty = reinterpret_cast<uint8_t *>(som + kHaloCap);
+    if (A.halo_hdr && halo_load<float4>(A, h, box, sps, ps, som, omega, sty))
+        apply_body(A, HaloSpace<float4>{sps, som, sty, box, h}, ps, omega, vx, v, x, hout);
+    else
+        apply_body(A, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
 }
 
 // Colour diffusion of the ref profile (oclsph_kernel.h:281-303): each fluid particle
@@ -1054,11 +1397,24 @@ GatherArgs gather_args(const StepView &s) {
     A.hcount = s.hcount;
     A.hcap = s.hlist ? s.hcap : 0;
     // near rows need the displacement bound (Verlet lists) and hit rows
-    A.near = s.cap && A.hcap ? s.near : nullptr;
+    A.near = s.cap && A.hcap && s.slack && s.dstep ? s.near : nullptr;
+    A.slack = s.slack;
+    A.dstep = s.dstep;
     A.near_r2 = s.near_r2;
     A.near_skin = s.near_skin;
     A.over = s.over;
+    A.near_stats = A.near ? s.near_stats : nullptr;
+    // the halo needs the list-build pass (which builds it) and CTAs of kHaloThreads
+    const bool halo = s.halo_hdr && s.halo_box && s.cap && s.block == (int)kHaloThreads;
+    A.halo_hdr = halo ? reinterpret_cast<HaloHdr *>(s.halo_hdr) : nullptr;
+    A.halo_box = halo ? s.halo_box : nullptr;
     return A;
+}
+
+// dynamic shared memory of a gather launch: the halo's, or none without it
+template <class T, bool kTypes>
+size_t smem_of(const GatherArgs &A) {
+    return A.halo_hdr ? halo_smem_bytes<T, kTypes>() : 0;
 }
 
 }  // namespace
@@ -1105,16 +1461,17 @@ void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStrea
     const GatherArgs A = gather_args(s);
     const unsigned g = grid_for(s.n, s.block);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
+    const size_t sm = smem_of<char, false>(A);
     if (iteration == 0 && A.cap) {
-        k_build_lists<<<g, s.block, 0, st>>>(A, ps);
-        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        k_build_lists<<<g, s.block, sm, st>>>(A, ps);
+        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
     } else if (iteration == 0) {
-        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
     } else {
-        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
     }
 }
 
@@ -1124,21 +1481,43 @@ void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int it
     const unsigned g = grid_for(s.n, s.block);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
     const int l = last ? 1 : 0;
+    const size_t sm = smem_of<float, false>(A);
     if (iteration == 0) {
-        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     } else {
-        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     }
 }
 
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {
     const GatherArgs A = gather_args(s);
     const unsigned g = grid_for(s.n, s.block);
-    k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
+    const size_t sm = smem_of<float4, true>(A);
+    k_vorticity_xsph<<<g, s.block, sm, st>>>(A, ps, s.v1, s.omega, s.vx);
     if (between) between();
-    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
+    k_vorticity_apply<<<g, s.block, sm, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
+}
+
+uint64_t halo_header_bytes(uint64_t n) { return ((n + kHaloThreads - 1) / kHaloThreads) * sizeof(HaloHdr); }
+uint64_t halo_box_bytes(uint64_t n) { return ((n + kHaloThreads - 1) / kHaloThreads) * kHaloBox * sizeof(uint2); }
+uint32_t halo_threads() { return kHaloThreads; }
+
+uint32_t halo_count(const void *host_headers, uint64_t ctas) {
+    const HaloHdr *h = static_cast<const HaloHdr *>(host_headers);
+    uint32_t k = 0;
+    for (uint64_t i = 0; i < ctas; ++i) k += h[i].ok ? 1u : 0u;
+    return k;
+}
+
+// The gather kernels' dynamic shared memory above the default 48 KB (the vorticity
+// passes stage two float4 arrays); set once per device, before any graph capture.
+cudaError_t halo_setup() {
+    const int big = (int)halo_smem_bytes<float4, true>();
+    cudaError_t e = cudaFuncSetAttribute(k_vorticity_xsph, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vorticity_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    return e;
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

@@ -277,7 +277,10 @@ std::once_flag g_tables_once[64];
 void ensure_tables() {
     int dev = 0;
     cudaGetDevice(&dev);
-    std::call_once(g_tables_once[dev & 63], [] { mc_tables_upload(); });
+    std::call_once(g_tables_once[dev & 63], [] {
+        mc_tables_upload();
+        halo_setup();
+    });
 }
 
 }  // namespace
@@ -499,8 +502,11 @@ struct fgb_batch {
     Pinned<HostParticlesOut> st_hout;
     // rows that overflowed in each step's build pass, copied to st_over at the end of
     // the step; grow_rows() enlarges the capacities when more than 1% did
+    // over[2..3]: near-row statistics of the checked passes (FGB_ROW_STATS=1), kept
+    // on the device across steps until fgb_batch_row_stats reads and clears them
     Dev<uint32_t> over;
     Pinned<uint32_t> st_over;
+    bool row_stats = false;
     // the device error flags (err) as of the end of each step, copied by the step
     // graph; fgb_batch_step, fgb_batch_sync and fgb_advance turn them into a status
     Pinned<uint32_t> st_flags;
@@ -516,8 +522,8 @@ struct fgb_batch {
     Dev<float4> ps_grid;
     Dev<uint32_t> nlist;
     Dev<uint16_t> ncount;
-    Dev<float> disp;
-    Dev<uint32_t> cellmax;
+    Dev<float> disp, dstep, slack;
+    Dev<uint2> cellmax;
     Dev<uint8_t> valid;
     Dev<uint32_t> hlist;
     Dev<uint16_t> hcount;
@@ -527,11 +533,21 @@ struct fgb_batch {
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
     int block = 128;  // threads per CTA of the gather kernels
+    // the gathers' shared-memory halo (pbf.cu): per-CTA boxes of the step, built by the
+    // list-build pass; needs the Verlet lists and CTAs of halo_threads() particles
+    bool halo = false;
+    Dev<char> halo_hdr, halo_box;
+    uint64_t steps_done = 0;
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
     Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
     Dev<uint32_t> colour_count;
     Dev<uint32_t> err;
+    // cell queries: the cell table is the last step's grid until the next upload, edit
+    // or surface replaces it
+    bool query_ok = false;
+    Dev<fgb_query> q_dev;
+    Dev<uint32_t> q_out;
     // surface
     bool surf_ready = false;
     uint64_t lat_total = 0, cube_total = 0;
@@ -620,18 +636,24 @@ struct fgb_batch {
         s.skin = skin;
         s.ps_grid = ps_grid.p;
         s.disp = disp.p;
+        s.dstep = dstep.p;
+        s.slack = slack.p;
         s.cellmax = cellmax.p;
         s.valid = valid.p;
         s.hlist = hlist.p;
         s.hcount = hcount.p;
         s.hcap = hlist.p ? hit_cap : 0;
-        const float near_skin = near_frac * ph.h;
+        // a near row filtered from a Verlet list is complete out to h + skin only
+        const float near_skin = std::min(near_frac, skin_frac) * ph.h;
         const float near_reach = (ph.h + near_skin) * 1.00001f;
         s.near = near_frac > 0.f ? near.p : nullptr;
         s.near_r2 = near_reach * near_reach;
         s.near_skin = near_skin;
         s.hout = advance_io ? hout_dev.p : nullptr;
         s.over = over.p;
+        s.near_stats = row_stats && over.p ? over.p + 2 : nullptr;
+        s.halo_hdr = halo ? (void *)halo_hdr.p : nullptr;
+        s.halo_box = halo ? (uint2 *)halo_box.p : nullptr;
         return s;
     }
 
@@ -665,7 +687,7 @@ struct fgb_batch {
         mark(k, st);
         if (io_up) FGB_CUDA(cudaStreamWaitEvent(st, io_up, cudaEventWaitExternal), "step: upload event");
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
-        if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
+        if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint2), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
         if (ph.profile == FGB_PROFILE_REF) {
@@ -685,7 +707,7 @@ struct fgb_batch {
             // starts from the clear above), so an iteration that overshoots does not keep
             // lists invalid after the next one has moved the particles back
             if (it > 0 && cellmax.p)
-                FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
+                FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint2), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
             l += (it == 0 && s.cap) ? 3 : 2;
@@ -739,6 +761,7 @@ struct fgb_batch {
         float best_skin = skin_frac, best_ms = 3.4e38f, ms = 0.f;
         const float skin0 = skin_frac;
         for (int blk : {64, 128, 256}) {
+            if (halo && blk != (int)halo_threads()) continue;  // the halo fixes the CTA size
             rc = trial(blk, skin0, &ms);
             if (rc) break;
             if (ms < best_ms) best_ms = ms, best_block = blk;
@@ -889,7 +912,9 @@ struct fgb_batch {
             FGB_CUDA(cudaGraphLaunch(graph[cur], stream()), "graph launch");
             cur ^= 1;
             launches += launches_per_step;
+            steps_done++;
         }
+        if (steps) query_ok = true;
         return FGB_OK;
     }
 
@@ -917,6 +942,7 @@ struct fgb_batch {
         int rc = sync_tris();  // the scene table (obstacle counts) as of the last upload
         if (!rc) rc = ensure_surface();
         if (rc) return rc;
+        query_ok = false;  // the cell table becomes the grid of the current positions
         cudaStream_t st = stream();
         StepView s = view(cur);
         s.keys_prev = keys_sorted.p;
@@ -1052,9 +1078,17 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
         FGB_CUDA(b->hlist.alloc(cap * b->hit_cap), "batch alloc hit lists");
         FGB_CUDA(b->hcount.alloc(cap), "batch alloc");
     }
-    if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
+    if (b->list_cap && b->hit_cap) {
+        FGB_CUDA(b->near.alloc(cap), "batch alloc");
+        FGB_CUDA(b->dstep.alloc(cap), "batch alloc");
+        FGB_CUDA(b->slack.alloc(cap), "batch alloc");
+    }
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
+    if (b->halo) {
+        FGB_CUDA(b->halo_hdr.alloc(halo_header_bytes(cap)), "batch alloc halo");
+        FGB_CUDA(b->halo_box.alloc(halo_box_bytes(cap)), "batch alloc halo");
+    }
     if (p.profile != FGB_PROFILE_REF) {
         FGB_CUDA(b->omega.alloc(cap), "batch alloc");
         FGB_CUDA(b->vx.alloc(cap), "batch alloc");
@@ -1175,13 +1209,23 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_NEAR_SKIN")) b->near_frac = (float)atof(e);
     if (b->hit_cap > 4096) b->hit_cap = 4096;
     b->hit_cap = (b->hit_cap + 3u) & ~3u;  // rows move as 16-byte vectors
+    {
+        // "1": the gathers read their neighbours from a shared-memory halo (pbf.cu);
+        // off by default, as it measured slower than reads through L1
+        const char *e = getenv("FGB_HALO");
+        b->halo = b->list_cap && e && strcmp(e, "1") == 0;
+        if (b->halo) b->block = (int)halo_threads();
+    }
     int rc = alloc_step_arrays(b, n);
     if (rc) return rc;
     FGB_CUDA(b->err.alloc(1), "batch alloc");
     FGB_CUDA(b->st_flags.ensure(1), "batch alloc");
     b->st_flags.p[0] = 0;
     if (b->list_cap || b->hit_cap) {
-        FGB_CUDA(b->over.alloc(2), "batch alloc");
+        FGB_CUDA(b->over.alloc(4), "batch alloc");
+        FGB_CUDA(cudaMemset(b->over.p, 0, 4 * sizeof(uint32_t)), "batch alloc");
+        const char *e = getenv("FGB_ROW_STATS");
+        b->row_stats = e && strcmp(e, "1") == 0;
         FGB_CUDA(b->st_over.ensure(2), "batch alloc");
         b->st_over.p[0] = b->st_over.p[1] = 0;
     }
@@ -1248,6 +1292,7 @@ static int sync_ids(fgb_batch *b) {
 // obstacles, and the scene's key prefix is set in case a surface call precedes
 // the first step.
 static void upload_done(fgb_batch *b, uint32_t k, uint32_t obstacles) {
+    b->query_ok = false;
     if (b->h_scenes[k].obstacles != obstacles) {
         b->h_scenes[k].obstacles = obstacles;
         b->tris_dirty = true;  // re-uploads the scene table before the next step
@@ -1344,6 +1389,7 @@ static int batch_copy_scene(fgb_batch *dst, uint32_t dk, fgb_batch *src, uint32_
     if (rc) return rc;
     FGB_CUDA(cudaStreamSynchronize(src->stream()), "copy_scene sync");
     dst->ids_stale[dk] = 0;  // the copy below brings the ids
+    dst->query_ok = false;
     const int cd = dst->cur, cs = src->cur;
     if (dst->h_scenes[dk].obstacles != src->h_scenes[sk].obstacles) {
         dst->h_scenes[dk].obstacles = src->h_scenes[sk].obstacles;
@@ -1527,7 +1573,8 @@ int fgb_struct_sizes(uint64_t *out, int n) {
                               sizeof(fgb_triangle), sizeof(fgb_mesh_triangle), sizeof(fgb_mesh),
                               sizeof(fgb_grid_info), sizeof(fgb_well),          sizeof(fgb_serve_options),
                               sizeof(fgb_serve_result), sizeof(fgb_serve_stats), sizeof(fgb_tune_result),
-                              sizeof(fgb_source),       sizeof(fgb_drain)};
+                              sizeof(fgb_source),       sizeof(fgb_drain),       sizeof(fgb_query),
+                              sizeof(fgb_query_result), sizeof(fgb_records)};
     const int m = (int)(sizeof(sizes) / sizeof(sizes[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = sizes[i];
     return m;
@@ -1814,6 +1861,34 @@ int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
     return FGB_OK;
 }
 
+int fgb_batch_row_stats(fgb_batch *b, uint32_t *near_warps, uint32_t *filter_warps) {
+    if (!b || !near_warps || !filter_warps) return fail(FGB_ERR_INVALID, "row_stats: bad argument");
+    *near_warps = *filter_warps = 0;
+    if (!b->row_stats || !b->over.p) return FGB_OK;
+    uint32_t h[2] = {0, 0};
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemcpyAsync(h, b->over.p + 2, sizeof(h), cudaMemcpyDeviceToHost, st), "row_stats");
+    FGB_CUDA(cudaMemsetAsync(b->over.p + 2, 0, sizeof(h), st), "row_stats");
+    FGB_CUDA(cudaStreamSynchronize(st), "row_stats");
+    *near_warps = h[0];
+    *filter_warps = h[1];
+    return FGB_OK;
+}
+
+int fgb_batch_halo_usage(fgb_batch *b, uint32_t *ctas, uint32_t *halo_ctas) {
+    if (!b || !ctas || !halo_ctas) return fail(FGB_ERR_INVALID, "halo_usage: bad argument");
+    *ctas = *halo_ctas = 0;
+    if (!b->halo || !b->halo_hdr.p || b->n == 0 || b->steps_done == 0) return FGB_OK;
+    const uint64_t n_ctas = (b->n + halo_threads() - 1) / halo_threads();
+    std::vector<char> host(halo_header_bytes(b->n));
+    cudaStream_t st = b->stream();
+    FGB_CUDA(cudaMemcpyAsync(host.data(), b->halo_hdr.p, host.size(), cudaMemcpyDeviceToHost, st), "halo_usage");
+    FGB_CUDA(cudaStreamSynchronize(st), "halo_usage");
+    *ctas = (uint32_t)n_ctas;
+    *halo_ctas = halo_count(host.data(), n_ctas);
+    return FGB_OK;
+}
+
 uint64_t fgb_batch_launch_count(const fgb_batch *b) { return b ? b->launches : 0; }
 
 int fgb_batch_autotune(fgb_batch *b, uint32_t steps_per_trial, fgb_tune_result *out) {
@@ -1903,6 +1978,7 @@ int fgb_batch_sources_drains(fgb_batch *b, uint32_t k, const fgb_source *sources
     if ((n_sources && !sources) || (n_drains && !drains)) return fail(FGB_ERR_INVALID, "sources_drains: null array");
     const fgb_config &c = b->cfg[k];
     PoolScope scope(&b->solver->pool);
+    b->query_ok = false;
     // emission (oclsph.hpp:678-691), with the drain test of 694-705 applied to the
     // new particles right away, as the reference erases after emitting
     const float spacing = (b->solver->params.h * c.scale / 2);
@@ -2081,6 +2157,46 @@ int fgb_batch_grid_info(fgb_batch *b, uint32_t scene, fgb_grid_info *out) {
     return FGB_OK;
 }
 
+// Cell queries of scene k against the grid of the batch's last step (query.cu); the
+// results of points whose cell holds fluid, in query order.  Synchronous.
+static int batch_query(fgb_batch *b, uint32_t k, const fgb_query *q, size_t nq, fgb_query_result *out,
+                       size_t *n_out) {
+    *n_out = 0;
+    if (!nq) return FGB_OK;
+    if (!b->query_ok)
+        return fail(FGB_ERR_INVALID, "query: the cell table is not a step's grid (no step since the last upload, "
+                                     "edit or surface)");
+    if (nq > 0xffffffffull) return fail(FGB_ERR_CAPACITY, "query: more than 2^32-1 queries");
+    cudaStream_t st = b->stream();
+    if (b->q_dev.n < nq || !b->q_dev.p) {
+        PoolScope scope(&b->solver->pool);
+        FGB_CUDA(b->q_dev.alloc(nq), "query alloc");
+        FGB_CUDA(b->q_out.alloc(2 * nq), "query alloc");
+    }
+    FGB_CUDA(cudaMemcpyAsync(b->q_dev.p, q, nq * sizeof(fgb_query), cudaMemcpyHostToDevice, st), "query upload");
+    const int cur = b->cur;
+    // the sorted types of the step, and the colours it started from (before its
+    // diffusion) through the sort's order
+    launch_queries(b->d_scenes.p, k, b->ph.h, b->cells.p, b->type[cur].p, b->vals_sorted.p, b->col[cur ^ 1].p,
+                   b->q_dev.p, (uint32_t)nq, b->q_out.p, b->q_out.p + nq, st);
+    FGB_CUDA(cudaGetLastError(), "query kernel");
+    std::vector<uint32_t> res(2 * nq);
+    FGB_CUDA(cudaMemcpyAsync(res.data(), b->q_out.p, 2 * nq * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+             "query download");
+    FGB_CUDA(cudaStreamSynchronize(st), "query sync");
+    size_t m = 0;
+    for (size_t i = 0; i < nq; ++i) {
+        if (!res[i]) continue;  // oclsph.hpp:789: only points whose cell holds fluid
+        fgb_query_result &r = out[m++];
+        r.id = q[i].id;
+        for (int a = 0; a < 3; ++a) r.point[a] = q[i].point[a];
+        r.neighbours = res[i];
+        r.average_colour = res[nq + i];
+    }
+    *n_out = m;
+    return FGB_OK;
+}
+
 // fgb_advance with direct host I/O: one frame with a single wait at its end.  The
 // upload and the download are split by when the step needs (or finishes) each field:
 //   main stream: positions, velocities, masses, types in (obstacles counted into the
@@ -2143,24 +2259,22 @@ static int advance_direct(fgb_batch *b, const fgb_config *cfg, fgb_particles *xs
     return advance_flags(b);
 }
 
-int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const fgb_triangle *colliders,
-                size_t n_colliders, fgb_mesh *mesh_out) {
-    if (!s || !cfg || !xs) return fail(FGB_ERR_INVALID, "advance: null argument");
-    if (n_colliders && !colliders) return fail(FGB_ERR_INVALID, "advance: null colliders");
-    if (mesh_out) mesh_out->n = 0;
-    if (xs->n == 0) return FGB_OK;  // oclsph.hpp:711-715 returns an empty result
+// The solver's single-scene batch for a frame of n particles under cfg, created when
+// the count or the configuration changed, with the frame's colliders and cleared
+// error flags.
+static int frame_batch(fgb_solver *s, const fgb_config *cfg, uint64_t n, const fgb_triangle *colliders,
+                       size_t n_colliders, fgb_batch **out) {
     // `surface` only says whether this frame also extracts a surface: it does not
     // change the resident scene, so frames that differ in it reuse the same batch
     fgb_config key = *cfg;
     key.surface = s->cached_cfg.surface;
-    const bool same = s->cached && s->cached_n == xs->n && memcmp(&s->cached_cfg, &key, sizeof(fgb_config)) == 0;
+    const bool same = s->cached && s->cached_n == n && memcmp(&s->cached_cfg, &key, sizeof(fgb_config)) == 0;
     if (!same) {
         if (s->cached) destroy_batch(s->cached);
         s->cached = nullptr;
-        uint64_t n = xs->n;
         int rc = fgb_batch_create(s, 1, &n, cfg, &s->cached);
         if (rc) return rc;
-        s->cached_n = xs->n;
+        s->cached_n = n;
         s->cached_cfg = *cfg;
         fgb_batch *nb = s->cached;
         if (nb->direct) {  // before the first step captures the graphs
@@ -2178,6 +2292,19 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     // previous frame has finished, so the pinned copy is not being written)
     b->st_flags.p[0] = 0;
     FGB_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(uint32_t), b->stream()), "advance: error flags");
+    *out = b;
+    return FGB_OK;
+}
+
+int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const fgb_triangle *colliders,
+                size_t n_colliders, fgb_mesh *mesh_out) {
+    if (!s || !cfg || !xs) return fail(FGB_ERR_INVALID, "advance: null argument");
+    if (n_colliders && !colliders) return fail(FGB_ERR_INVALID, "advance: null colliders");
+    if (mesh_out) mesh_out->n = 0;
+    if (xs->n == 0) return FGB_OK;  // oclsph.hpp:711-715 returns an empty result
+    fgb_batch *b = nullptr;
+    int rc = frame_batch(s, cfg, xs->n, colliders, n_colliders, &b);
+    if (rc) return rc;
     if (b->advance_io && b->io_stream) return advance_direct(b, cfg, xs, mesh_out);
     rc = batch_upload(b, 0, xs);
     if (rc) return rc;
@@ -2189,6 +2316,150 @@ int fgb_advance(fgb_solver *s, const fgb_config *cfg, fgb_particles *xs, const f
     }
     rc = batch_download(b, 0, xs);
     return rc ? rc : advance_flags(b);
+}
+
+// fgb_advance_records with direct host I/O: one kernel reads the caller's records
+// before the step (a tile of records staged in shared memory), the step's last
+// kernel stores the final positions and velocities into them, and io_stream writes
+// type, colour, id and mass once the grid is built, while the gathers run.  The
+// queries are answered between the step and the surface, while the cell table is
+// the step's grid.
+static int advance_records_direct(fgb_batch *b, const fgb_config *cfg, const HostRecords &r, uint64_t n,
+                                  const fgb_query *queries, size_t n_queries, fgb_query_result *results,
+                                  size_t *n_results, fgb_mesh *mesh_out) {
+    int rc = b->sync_tris();  // the scene table before the upload counts obstacles into it
+    if (rc) return rc;
+    cudaStream_t st = b->stream(), io = b->io_stream;
+    const int c = b->cur, next = c ^ 1;
+    uint32_t *obstacles = &b->d_scenes.p[0].obstacles;
+    // the records are inputs and outputs: their pages are readied, contents kept,
+    // before any kernel of the frame reads or stores into them
+    ready_pages({{r.base, n * r.stride}}, true);
+    FGB_CUDA(cudaMemsetAsync(obstacles, 0, sizeof(uint32_t), st), "advance: upload");
+    launch_pack_records(r, n, b->x[c].p, b->v[c].p, b->type[c].p, b->col[c].p, b->slot[c].p, b->ids_dev.p, obstacles,
+                        st);
+    FGB_CUDA(cudaGetLastError(), "advance: upload kernel");
+    FGB_CUDA(cudaEventRecord(b->io_up, st), "advance: upload event");  // every field is in
+    launch_fill_u32(b->keys_sorted.p, n, 0u, st);  // scene 0's key prefix for the prediction
+    b->ids[0].clear();
+    b->ids_stale[0] = 0;
+    b->query_ok = false;
+    b->st_hout.p[0] = record_fields(r, true, false);
+    FGB_CUDA(cudaMemcpyAsync(b->hout_dev.p, b->st_hout.p, sizeof(HostParticlesOut), cudaMemcpyHostToDevice, st),
+             "advance: output records");
+    rc = b->step(1);
+    if (rc) return rc;
+    FGB_CUDA(cudaStreamWaitEvent(io, b->grid_ready, 0), "advance: io wait");
+    launch_unpack_static(record_fields(r, false, true), n, b->ps_grid.p, b->type[next].p, b->col[next].p,
+                         b->slot[next].p, b->ids_dev.p, io);
+    FGB_CUDA(cudaGetLastError(), "advance: download kernel");
+    FGB_CUDA(cudaEventRecord(b->io_done, io), "advance: io event");
+    if (n_queries) {
+        rc = batch_query(b, 0, queries, n_queries, results, n_results);
+        if (rc) return rc;
+    }
+    if (cfg->surface && mesh_out) {
+        rc = fgb_batch_surface(b, 0, mesh_out);
+        if (rc) return rc;
+    }
+    FGB_CUDA(cudaMemcpyAsync(b->st_count.p, obstacles, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+             "advance: obstacle count");
+    FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
+    FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
+    b->h_scenes[0].obstacles = b->st_count.p[0];  // the device table has it already
+    return advance_flags(b);
+}
+
+int fgb_advance_records(fgb_solver *s, const fgb_config *cfg, fgb_records *xs, const fgb_triangle *colliders,
+                        size_t n_colliders, const fgb_query *queries, size_t n_queries, fgb_query_result *results,
+                        size_t *n_results, fgb_mesh *mesh_out) {
+    if (!s || !cfg || !xs) return fail(FGB_ERR_INVALID, "advance_records: null argument");
+    if (n_colliders && !colliders) return fail(FGB_ERR_INVALID, "advance_records: null colliders");
+    if (n_queries && (!queries || !results || !n_results))
+        return fail(FGB_ERR_INVALID, "advance_records: queries need results and n_results");
+    if (n_results) *n_results = 0;
+    if (mesh_out) mesh_out->n = 0;
+    const uint32_t st = xs->stride;
+    auto field_ok = [&](int32_t off, uint32_t bytes, bool required) {
+        if (off < 0) return !required;
+        return (off % 4) == 0 && (uint64_t)off + bytes <= st;
+    };
+    if (st == 0 || st % 4 || st > kMaxRecordStride || ((uintptr_t)xs->base % 4) ||
+        (xs->id_bytes != 4 && xs->id_bytes != 8) || !field_ok(xs->position, 12, true) ||
+        !field_ok(xs->velocity, 12, true) || !field_ok(xs->mass, 4, true) || !field_ok(xs->type, 4, true) ||
+        !field_ok(xs->colour, 4, false) || !field_ok(xs->id, xs->id_bytes, false))
+        return fail(FGB_ERR_INVALID, "advance_records: the record layout must have a stride of at most 128 bytes, "
+                                     "4-byte aligned fields within it, and position, velocity, mass and type");
+    if (xs->n && !xs->base) return fail(FGB_ERR_INVALID, "advance_records: null records");
+    if (xs->n == 0) return FGB_OK;  // oclsph.hpp:711-715 returns an empty result
+    fgb_batch *b = nullptr;
+    int rc = frame_batch(s, cfg, xs->n, colliders, n_colliders, &b);
+    if (rc) return rc;
+    const HostRecords r{(char *)xs->base, st, xs->id_bytes, xs->id, xs->type, xs->mass, xs->position, xs->velocity,
+                        xs->colour};
+    const uint64_t n = xs->n;
+    if (b->advance_io && b->io_stream)
+        return advance_records_direct(b, cfg, r, n, queries, n_queries, results, n_results, mesh_out);
+    // staged: the records to and from packed arrays on the host threads, around the
+    // packed-array frame
+    std::vector<uint64_t> id(n);
+    std::vector<int32_t> type(n);
+    std::vector<float> mass(n), pos(3 * n), vel(3 * n);
+    std::vector<uint32_t> col(n);
+    auto word = [&](uint64_t i, int32_t off) { return (const void *)(r.base + i * st + off); };
+    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            memcpy(&pos[3 * i], word(i, r.off_position), 12);
+            memcpy(&vel[3 * i], word(i, r.off_velocity), 12);
+            memcpy(&mass[i], word(i, r.off_mass), 4);
+            memcpy(&type[i], word(i, r.off_type), 4);
+            col[i] = 0xffffffffu;
+            if (r.off_colour >= 0) memcpy(&col[i], word(i, r.off_colour), 4);
+            id[i] = i;
+            if (r.off_id >= 0) {
+                if (r.id_bytes == 8) {
+                    memcpy(&id[i], word(i, r.off_id), 8);
+                } else {
+                    uint32_t v;
+                    memcpy(&v, word(i, r.off_id), 4);
+                    id[i] = v;
+                }
+            }
+        }
+    });
+    fgb_particles p{n, id.data(), type.data(), mass.data(), pos.data(), vel.data(), col.data()};
+    rc = batch_upload(b, 0, &p);
+    if (!rc) rc = b->step(1);
+    if (!rc && n_queries) rc = batch_query(b, 0, queries, n_queries, results, n_results);
+    if (!rc && cfg->surface && mesh_out) rc = fgb_batch_surface(b, 0, mesh_out);
+    if (!rc) rc = batch_download(b, 0, &p);
+    if (rc) return rc;
+    parallel_for(n, [&](uint64_t lo, uint64_t hi) {
+        for (uint64_t i = lo; i < hi; ++i) {
+            char *rec = r.base + i * st;
+            memcpy(rec + r.off_position, &pos[3 * i], 12);
+            memcpy(rec + r.off_velocity, &vel[3 * i], 12);
+            memcpy(rec + r.off_mass, &mass[i], 4);
+            memcpy(rec + r.off_type, &type[i], 4);
+            if (r.off_colour >= 0) memcpy(rec + r.off_colour, &col[i], 4);
+            if (r.off_id >= 0) {
+                if (r.id_bytes == 8) {
+                    memcpy(rec + r.off_id, &id[i], 8);
+                } else {
+                    const uint32_t v = (uint32_t)id[i];
+                    memcpy(rec + r.off_id, &v, 4);
+                }
+            }
+        }
+    });
+    return advance_flags(b);
+}
+
+int fgb_batch_query(fgb_batch *b, uint32_t scene, const fgb_query *queries, size_t n, fgb_query_result *results,
+                    size_t *n_results) {
+    if (!b || !n_results || scene >= b->n_scenes || (n && (!queries || !results)))
+        return fail(FGB_ERR_INVALID, "query: bad argument");
+    return batch_query(b, scene, queries, n, results, n_results);
 }
 
 int fgb_host_ready_pages(void *p, size_t bytes, int keep_contents, uint64_t *touched) {

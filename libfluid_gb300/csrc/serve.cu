@@ -4,9 +4,10 @@
 // A worker thread admits waiting requests in arrival order while their device
 // footprint fits the HBM budget and keeps every admitted scene resident on the
 // device.  Admitted scenes are spread over groups of at most tick_particles
-// particles; one tick advances one group by one step (one launch per stage for all
-// its scenes, fgb_batch_step), taking the groups round robin.  A tick's latency is
-// linear in its particles (~0.27 ms + 2.9 ns a particle on GB300), so the groups are
+// particles; one tick advances one group (one launch per stage for all its scenes,
+// fgb_batch_step), taking the groups round robin: by one step, or by several when the
+// group is small (tick_steps).  A tick's latency is linear in its particle-steps
+// (~0.3 ms + 3.2 ns a particle-step on GB300), so the groups are
 // kept as few and as even as the scenes allow: a new scene joins the lightest group
 // it fits, and whenever the groups are uneven (or more than ceil(total /
 // tick_particles) of them exist) the scenes are re-spread largest first onto the
@@ -104,6 +105,8 @@ struct fgb_server {
     double busy = 0, rebuild_time = 0;
     std::vector<double> step_latency;
     std::vector<uint64_t> step_particles;  // particles of each tick, beside step_latency
+    std::vector<uint32_t> step_scenes;     // scenes (requests) stepped by each tick
+    std::vector<uint32_t> step_count;      // steps each tick advanced its group by
     std::vector<double> step_start;        // start of each tick, seconds since creation
     std::string last_error;
 
@@ -312,24 +315,51 @@ struct fgb_server {
         g.particles = 0;
     }
 
-    // One tick: step group g once; finished scenes run their surface and go home.
+    // Steps of the next tick of g.  A tick costs about kTickFixed + n particles of
+    // work (0.3 ms + 3.2 ns a particle on GB300, measured), so a group below half of
+    // tick_particles takes k steps with k (n + kTickFixed) <= tick_particles +
+    // kTickFixed: every tick then does between half and all of a full group's work,
+    // and its latency stays within a factor of two whatever the load.  k never takes
+    // a scene past its last step, and a tick that would leave a scene a remainder
+    // shorter than k takes the remainder's share now (two even ticks, not a long one
+    // and a short one).
+    static constexpr uint64_t kTickFixed = 98304;
+    uint32_t tick_steps(const ServeGroup &g) const {
+        if (opt.one_at_a_time || opt.max_steps_per_tick <= 1) return 1;
+        uint64_t n = 0;
+        uint32_t rest = UINT32_MAX;
+        for (const Request *r : g.scenes) {
+            n += r->n;
+            rest = std::min(rest, r->remaining);
+        }
+        uint64_t k = (opt.tick_particles + kTickFixed) / (n + kTickFixed);
+        k = std::max<uint64_t>(1, std::min<uint64_t>(k, opt.max_steps_per_tick));
+        if (k >= rest) return rest;
+        if (rest < 2 * k) k = (rest + 1) / 2;
+        return (uint32_t)k;
+    }
+
+    // One tick: step group g tick_steps(g) times; finished scenes run their surface
+    // and go home.
     void tick(ServeGroup &g) {
+        const uint32_t k = tick_steps(g);
         const double s0 = now_s();
-        int rc = fgb_batch_step(g.batch, 1);
+        int rc = fgb_batch_step(g.batch, k);
         if (!rc) rc = fgb_batch_sync(g.batch);
         const double s1 = now_s();
         if (rc) return fail_group(g, rc);
         std::vector<Request *> done;
-        for (size_t k = 0; k < g.scenes.size(); ++k) {
-            Request *r = g.scenes[k];
-            if (--r->remaining) continue;
+        for (size_t j = 0; j < g.scenes.size(); ++j) {
+            Request *r = g.scenes[j];
+            r->remaining -= k;
+            if (r->remaining) continue;
             if (r->want_mesh) {
-                rc = fgb_batch_surface(g.batch, (uint32_t)k, &r->mesh);
+                rc = fgb_batch_surface(g.batch, (uint32_t)j, &r->mesh);
                 if (rc) return fail_group(g, rc);
                 r->triangles = r->mesh.n;
             }
             fgb_particles v = r->view();
-            rc = fgb_batch_download(g.batch, (uint32_t)k, &v);
+            rc = fgb_batch_download(g.batch, (uint32_t)j, &v);
             if (rc) return fail_group(g, rc);
             done.push_back(r);
         }
@@ -352,8 +382,10 @@ struct fgb_server {
         ticks++;
         uint64_t tick_n = 0;
         for (Request *r : g.scenes) tick_n += r->n;
-        particle_steps += tick_n;
+        particle_steps += tick_n * k;
         step_particles.push_back(tick_n);
+        step_scenes.push_back((uint32_t)g.scenes.size());
+        step_count.push_back(k);
         for (Request *r : done) {
             r->status = FGB_SERVE_DONE;
             r->t_done = t();
@@ -430,6 +462,7 @@ int fgb_serve_create(fgb_solver *s, const fgb_serve_options *opt, fgb_server **o
     if (!sv->opt.budget_bytes) sv->opt.budget_bytes = 150ull << 30;
     if (!sv->opt.max_active) sv->opt.max_active = 256;
     if (!sv->opt.tick_particles) sv->opt.tick_particles = 2097152;
+    if (!sv->opt.max_steps_per_tick) sv->opt.max_steps_per_tick = 16;
     cudaGetDevice(&sv->device);
     sv->t0 = now_s();
     sv->worker = std::thread([sv] { sv->run(); });
@@ -543,6 +576,22 @@ int fgb_serve_step_latencies(fgb_server *sv, double *out, uint64_t max, uint64_t
     std::lock_guard<std::mutex> lk(sv->mu);
     *count = sv->step_latency.size();
     for (uint64_t i = 0; out && i < max && i < sv->step_latency.size(); ++i) out[i] = sv->step_latency[i];
+    return FGB_OK;
+}
+
+int fgb_serve_tick_scenes(fgb_server *sv, uint32_t *out, uint64_t max, uint64_t *count) {
+    if (!sv || !count) return fail(FGB_ERR_INVALID, "serve_tick_scenes: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->step_scenes.size();
+    for (uint64_t i = 0; out && i < max && i < sv->step_scenes.size(); ++i) out[i] = sv->step_scenes[i];
+    return FGB_OK;
+}
+
+int fgb_serve_tick_steps(fgb_server *sv, uint32_t *out, uint64_t max, uint64_t *count) {
+    if (!sv || !count) return fail(FGB_ERR_INVALID, "serve_tick_steps: null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->step_count.size();
+    for (uint64_t i = 0; out && i < max && i < sv->step_count.size(); ++i) out[i] = sv->step_count[i];
     return FGB_OK;
 }
 

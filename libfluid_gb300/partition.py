@@ -44,9 +44,11 @@ def local_scenes(specs, rank, world, size_of=None):
 
 class Router:
     """Serving front end over `world` ranks: a request goes to the rank with the
-    fewest outstanding particle-steps (ties to the lowest rank).  Every rank can run
-    the same router over the same request stream and reach the same routing, so no
-    message is needed to agree on it."""
+    fewest outstanding particle-steps (ties to the lowest rank).  A single front end
+    that sees completions reports them with done(); ranks that each run a copy over
+    the same request stream (route_stream) call route() alone, so that the copies
+    see the same history and agree on every request with no message: the balance is
+    then over the particle-steps assigned so far."""
 
     def __init__(self, world):
         self.outstanding = [0] * world
@@ -72,4 +74,52 @@ def gather_summary(obj):
         return [obj]
     out = [None] * dist.get_world_size()
     dist.all_gather_object(out, obj)
+    return out
+
+
+def route_stream(requests, rank, world, n_of=lambda r: r[1], steps_of=lambda r: r[2]):
+    """This rank's requests of a stream every rank holds in the same order: each
+    request routed by a Router that is never told of completions, so every rank
+    computes the same owner for every request.  Returns (position in the stream,
+    request) pairs."""
+    router = Router(world)
+    return [(k, r) for k, r in enumerate(requests) if router.route(k, n_of(r), steps_of(r)) == rank]
+
+
+def barrier():
+    """A barrier over the default process group, when there is one."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def sharded_run(specs, rank, world, run_local, size_of=None):
+    """The sharded form of a batch of independent scenes: this rank's share
+    (local_scenes) goes to run_local(list of (global index, spec)), which returns a
+    dict of host-side results; all ranks start together and the ranks' dicts are
+    exchanged once at the end.  Returns every rank's dict, indexed by rank; combine()
+    merges them."""
+    mine = local_scenes(specs, rank, world, size_of)
+    barrier()
+    local = run_local(mine)
+    local = dict(local, rank=rank, scenes=[i for i, _ in mine])
+    return gather_summary(local)
+
+
+def combine(per_rank, sum_keys=(), max_keys=(), merge_keys=(), concat_keys=()):
+    """One summary of a sharded run: sum_keys added over ranks (work done), max_keys
+    their maximum (the job's time is its slowest rank's), merge_keys dicts united
+    (results by global index), concat_keys lists joined in rank order."""
+    out = {"ranks": len(per_rank)}
+    for k in sum_keys:
+        out[k] = sum(r[k] for r in per_rank)
+    for k in max_keys:
+        out[k] = max(r[k] for r in per_rank)
+    for k in merge_keys:
+        m = {}
+        for r in per_rank:
+            m.update(r[k])
+        out[k] = m
+    for k in concat_keys:
+        out[k] = [x for r in per_rank for x in r[k]]
     return out

@@ -11,14 +11,17 @@ class Server:
 
     submit() copies a scene and returns a ticket; the library's worker thread admits
     scenes against the HBM budget, packs resident scenes into groups of at most
-    tick_particles particles, advances one group by one batched step per tick (round
-    robin) and, when a scene has run its steps, extracts its surface (on request)
-    and keeps its final state for fetch()."""
+    tick_particles particles, advances one group per tick (round robin) by one
+    batched step, or by up to max_steps_per_tick steps when the group holds less than
+    half of tick_particles, and, when a scene has run its steps, extracts its surface
+    (on request) and keeps its final state for fetch()."""
 
-    def __init__(self, solver, budget_bytes=150 << 30, max_active=256, one_at_a_time=False, tick_particles=0):
+    def __init__(self, solver, budget_bytes=150 << 30, max_active=256, one_at_a_time=False, tick_particles=0,
+                 max_steps_per_tick=0):
         self.solver = solver
         self.lib = solver.lib
-        opt = capi.ServeOptions(budget_bytes, max_active, 1 if one_at_a_time else 0, tick_particles)
+        opt = capi.ServeOptions(budget_bytes, max_active, 1 if one_at_a_time else 0, tick_particles,
+                                max_steps_per_tick)
         self._h = ctypes.c_void_p()
         capi.check(self.lib.fgb_serve_create(solver.handle, ctypes.byref(opt), ctypes.byref(self._h)))
         solver._servers.add(self)
@@ -73,6 +76,22 @@ class Server:
         buf = (ctypes.c_uint64 * max(cnt.value, 1))()
         capi.check(self.lib.fgb_serve_tick_particles(self._h, buf, cnt.value, ctypes.byref(cnt)))
         return np.frombuffer(buf, dtype=np.uint64)[:cnt.value].copy()
+
+    def tick_scenes(self):
+        """Requests stepped by each tick, aligned with step_latencies()."""
+        cnt = ctypes.c_uint64()
+        capi.check(self.lib.fgb_serve_tick_scenes(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_uint32 * max(cnt.value, 1))()
+        capi.check(self.lib.fgb_serve_tick_scenes(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        return np.frombuffer(buf, dtype=np.uint32)[:cnt.value].copy()
+
+    def tick_steps(self):
+        """Steps each tick advanced its group by, aligned with step_latencies()."""
+        cnt = ctypes.c_uint64()
+        capi.check(self.lib.fgb_serve_tick_steps(self._h, None, 0, ctypes.byref(cnt)))
+        buf = (ctypes.c_uint32 * max(cnt.value, 1))()
+        capi.check(self.lib.fgb_serve_tick_steps(self._h, buf, cnt.value, ctypes.byref(cnt)))
+        return np.frombuffer(buf, dtype=np.uint32)[:cnt.value].copy()
 
     def tick_starts(self):
         """Start of each tick, seconds since the server was created."""

@@ -69,6 +69,32 @@ class SphSolver:
         finally:
             self.lib.fgb_mesh_free(ctypes.byref(mesh))
 
+    def advance_records(self, config, records, colliders=None, queries=None):
+        """One frame on a numpy array of capi.PARTICLE_RECORD (read and written in
+        place, Morton order) with cell queries [(id, (x, y, z))]: returns (mesh or
+        None, [(id, point, neighbours, average_colour)])."""
+        rv = capi.records_view(records)
+        tris, ntris = _tri_array(colliders)
+        tp = tris.ctypes.data_as(_P(capi.Triangle)) if tris is not None else None
+        queries = list(queries or [])
+        nq = len(queries)
+        qs = (capi.Query * max(nq, 1))()
+        for i, (qid, pt) in enumerate(queries):
+            qs[i].id = qid
+            qs[i].point[:] = pt
+        res = (capi.QueryResult * max(nq, 1))()
+        nres = ctypes.c_size_t()
+        mesh = capi.Mesh()
+        rc = self.lib.fgb_advance_records(self._h, ctypes.byref(config), ctypes.byref(rv), tp, ntris, qs, nq, res,
+                                          ctypes.byref(nres), ctypes.byref(mesh))
+        try:
+            capi.check(rc)
+            out = [(int(res[i].id), tuple(res[i].point), int(res[i].neighbours), int(res[i].average_colour))
+                   for i in range(nres.value)]
+            return (capi.mesh_to_numpy(mesh) if config.surface else None), out
+        finally:
+            self.lib.fgb_mesh_free(ctypes.byref(mesh))
+
     def close(self):
         if self._h:
             # the library destroys the solver's batches with it
@@ -200,10 +226,36 @@ class Batch:
         capi.check(self.lib.fgb_batch_host_io(self._h, ctypes.byref(d)))
         return bool(d.value)
 
+    def query(self, k, queries):
+        """Cell queries [(id, (x, y, z))] of scene k against the grid of the last step."""
+        nq = len(queries)
+        qs = (capi.Query * max(nq, 1))()
+        for i, (qid, pt) in enumerate(queries):
+            qs[i].id = qid
+            qs[i].point[:] = pt
+        res = (capi.QueryResult * max(nq, 1))()
+        nres = ctypes.c_size_t()
+        capi.check(self.lib.fgb_batch_query(self._h, k, qs, nq, res, ctypes.byref(nres)))
+        return [(int(res[i].id), tuple(res[i].point), int(res[i].neighbours), int(res[i].average_colour))
+                for i in range(nres.value)]
+
     def error_flags(self):
         f = ctypes.c_uint32()
         capi.check(self.lib.fgb_batch_error_flags(self._h, ctypes.byref(f)))
         return int(f.value)
+
+    def halo_usage(self):
+        """(CTAs of the last step, CTAs that read neighbours from shared memory)."""
+        c, h = ctypes.c_uint32(), ctypes.c_uint32()
+        capi.check(self.lib.fgb_batch_halo_usage(self._h, ctypes.byref(c), ctypes.byref(h)))
+        return int(c.value), int(h.value)
+
+    def row_stats(self):
+        """(warps of checked passes on near rows, warps that filtered) since the last
+        call; zeros unless FGB_ROW_STATS=1 was set when the batch was created."""
+        a, b = ctypes.c_uint32(), ctypes.c_uint32()
+        capi.check(self.lib.fgb_batch_row_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
 
     def set_timing(self, on=True):
         capi.check(self.lib.fgb_batch_set_timing(self._h, 1 if on else 0))

@@ -91,6 +91,7 @@ typedef struct kc {
     float rho0, inv_rho0;
     float corr_ref; /* ref: poly6(dq)            oclsph_kernel.h:350 */
     float corr_wdq; /* baseline: (h^2 - dq^2)^3  (poly6 without its factor) */
+    float inv_corr_wdq; /* 1 / corr_wdq: s_corr's ratio is a product, no division per pair */
     float corr_k;   /* baseline: k * h^2 (s_corr carried in lambda's units, length^2) */
 } kc;
 
@@ -105,6 +106,7 @@ static void consts(const fgb_params *p, kc *k) {
     float dq = p->corr_delta_q * p->h;
     float t = k->hh - dq * dq;
     k->corr_wdq = t * t * t;
+    k->inv_corr_wdq = k->corr_wdq != 0.f ? 1.f / k->corr_wdq : 0.f;
     k->corr_ref = orc_poly6(p, dq);
     /* The PBF paper's s_corr = -k (W/W(dq))^n is dimensionless only in units where
      * h = 1; added to lambda (length^2) it is scaled by h^2 here. */
@@ -128,6 +130,10 @@ float orc_spiky_scale(const fgb_params *p, float r) {
 }
 
 /* s_corr ratio^n: n == 4 is evaluated as two squarings on CPU and GPU alike. */
+/* Squared distance in the baseline profile: two fused multiply-adds (the GPU's
+ * __fmaf_rn gives the same bits). */
+static inline float dist2(float dx, float dy, float dz) { return fmaf(dx, dx, fmaf(dy, dy, dz * dz)); }
+
 static inline float corr_pow(float ratio, float n) {
     if (n == 4.f) {
         float r2 = ratio * ratio;
@@ -412,7 +418,9 @@ static void lambda_pass(const state *s, const float *ps, float *lam, float *rho_
         for (int q = 0; q < R.n; ++q) {
             for (uint32_t b = R.r[q][0]; b < R.r[q][1]; ++b) {
                 float dx = ax - ps[3 * b], dy = ay - ps[3 * b + 1], dz = az - ps[3 * b + 2];
-                float r2 = dx * dx + dy * dy + dz * dz;
+                /* the ref profile sums three products as the reference does; the
+                 * baseline takes two fused multiply-adds */
+                float r2 = ref ? dx * dx + dy * dy + dz * dz : dist2(dx, dy, dz);
                 if (ref) {
                     float r = sqrtf(r2);
                     if (r <= k->h) {
@@ -487,7 +495,7 @@ static void delta_pass(const state *s, const float *ps, const float *lam, float 
         for (int q = 0; q < R.n; ++q) {
             for (uint32_t b = R.r[q][0]; b < R.r[q][1]; ++b) {
                 float dx = ax - ps[3 * b], dy = ay - ps[3 * b + 1], dz = az - ps[3 * b + 2];
-                float r2 = dx * dx + dy * dy + dz * dz;
+                float r2 = ref ? dx * dx + dy * dy + dz * dz : dist2(dx, dy, dz);
                 if (ref) {
                     float r = sqrtf(r2);
                     float w = 0.f;
@@ -509,7 +517,7 @@ static void delta_pass(const state *s, const float *ps, const float *lam, float 
                         float r = sqrtf(r2);
                         if (r >= KERNEL_EPSILON) {
                             float t = k->hh - r2;
-                            float corr = -k->corr_k * corr_pow((t * t * t) / k->corr_wdq, cn);
+                            float corr = -k->corr_k * corr_pow((t * t * t) * k->inv_corr_wdq, cn);
                             float hr = k->h - r;
                             float sc = s->mass[b] * ((hr * hr) / r) * (la + lam[b] + corr);
                             px = fmaf(sc, dx, px);
@@ -575,7 +583,7 @@ static void velocity_terms(const state *s, const float *ps, float *vel) {
             for (uint32_t b = R.r[q][0]; b < R.r[q][1]; ++b) {
                 if (s->type[b] == FGB_TYPE_OBSTACLE) continue;
                 float d[3] = {ax - ps[3 * b], ay - ps[3 * b + 1], az - ps[3 * b + 2]};
-                float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                float r2 = dist2(d[0], d[1], d[2]);
                 if (!(r2 <= k->hh)) continue;
                 float vab[3] = {vel[3 * b] - va[0], vel[3 * b + 1] - va[1], vel[3 * b + 2] - va[2]};
                 float t = k->hh - r2;
@@ -617,7 +625,7 @@ static void velocity_terms(const state *s, const float *ps, float *vel) {
             for (uint32_t b = R.r[q][0]; b < R.r[q][1]; ++b) {
                 if (s->type[b] == FGB_TYPE_OBSTACLE) continue;
                 float d[3] = {ax - ps[3 * b], ay - ps[3 * b + 1], az - ps[3 * b + 2]};
-                float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                float r2 = dist2(d[0], d[1], d[2]);
                 if (!(r2 <= k->hh)) continue;
                 float r = sqrtf(r2);
                 if (!(r >= KERNEL_EPSILON)) continue;

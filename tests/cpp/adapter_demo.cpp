@@ -31,7 +31,10 @@ int main() {
         sv += (double)p.velocity.x + 2.0 * p.velocity.y + 3.0 * p.velocity.z;
         sid = sid * 1000003ull + p.id;
     }
-    std::printf("{\"n\": %zu, \"pos\": %.9g, \"vel\": %.9g, \"id_hash\": %llu, \"triangles\": %zu, \"queries\": %zu}\n",
-                xs.size(), sp, sv, sid, result.triangles.size(), result.queries.size());
+    const size_t qn = result.queries.empty() ? 0 : result.queries[0].neighbours;
+    const unsigned qc = result.queries.empty() ? 0u : result.queries[0].averageColour;
+    std::printf("{\"n\": %zu, \"pos\": %.9g, \"vel\": %.9g, \"id_hash\": %llu, \"triangles\": %zu, \"queries\": %zu, "
+                "\"q_neighbours\": %zu, \"q_colour\": %u}\n",
+                xs.size(), sp, sv, sid, result.triangles.size(), result.queries.size(), qn, qc);
     return 0;
 }

@@ -22,11 +22,11 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_struct_sizes_match_ctypes(lib):
-    out = (ctypes.c_uint64 * 16)()
-    m = lib.fgb_struct_sizes(out, 16)
+    out = (ctypes.c_uint64 * 32)()
+    m = lib.fgb_struct_sizes(out, 32)
     ours = [capi.Params, capi.Config, capi.Particles, capi.Triangle, capi.MeshTriangle, capi.Mesh,
             capi.GridInfo, capi.Well, capi.ServeOptions, capi.ServeResult, capi.ServeStats, capi.TuneResult,
-            capi.Source, capi.Drain]
+            capi.Source, capi.Drain, capi.Query, capi.QueryResult, capi.Records]
     assert m == len(ours)
     for i, t in enumerate(ours):
         assert out[i] == ctypes.sizeof(t), (t.__name__, out[i], ctypes.sizeof(t))

@@ -50,8 +50,10 @@ def test_adapter_matches_c_abi(tmp_path):
     cfg.constant_force[:] = (0.0, -9.8, 0.0)
     cfg.max_bound[:] = (1.5, 1.5, 1.5)
     solver = SphSolver(profile=capi.PROFILE_REF)
+    rec = capi.to_records(parts)
     for _ in range(3):
-        mesh = solver.advance(cfg, parts)
+        mesh, results = solver.advance_records(cfg, rec, None, [(7, (0.3, 0.05, 0.3))])
+    parts = capi.from_records(rec)
     p = parts["position"].reshape(-1, 3).astype(np.float64)
     v = parts["velocity"].reshape(-1, 3).astype(np.float64)
     sp = float((p[:, 0] + 2 * p[:, 1] + 3 * p[:, 2]).sum())
@@ -64,5 +66,6 @@ def test_adapter_matches_c_abi(tmp_path):
     for i in parts["id"]:
         h = (h * 1000003 + int(i)) % (1 << 64)
     assert got["id_hash"] == h
-    assert got["queries"] == 1
+    assert got["queries"] == len(results) == 1
+    assert (got["q_neighbours"], got["q_colour"]) == (results[0][2], results[0][3])
     solver.close()

@@ -31,8 +31,9 @@ def _alone(solver, parts, cfg, steps, mesh):
     return got, tris
 
 
-def _serve(solver, reqs, one_at_a_time=False, stagger=0.0, tick_particles=0):
-    sv = Server(solver, budget_bytes=8 << 30, one_at_a_time=one_at_a_time, tick_particles=tick_particles)
+def _serve(solver, reqs, one_at_a_time=False, stagger=0.0, tick_particles=0, max_steps_per_tick=1):
+    sv = Server(solver, budget_bytes=8 << 30, one_at_a_time=one_at_a_time, tick_particles=tick_particles,
+                max_steps_per_tick=max_steps_per_tick)
     tickets = []
     for parts, cfg, steps, mesh in reqs:
         tickets.append(sv.submit(cfg, parts, steps, mesh))
@@ -43,21 +44,22 @@ def _serve(solver, reqs, one_at_a_time=False, stagger=0.0, tick_particles=0):
     st = sv.stats()
     lat = sv.step_latencies()
     # per-tick particles and start times line up with the latencies
-    tp, t0 = sv.tick_particles(), sv.tick_starts()
-    assert len(tp) == len(lat) == len(t0) == st.ticks
-    assert int(tp.sum()) == st.particle_steps
+    tp, t0, ks = sv.tick_particles(), sv.tick_starts(), sv.tick_steps()
+    assert len(tp) == len(lat) == len(t0) == len(ks) == st.ticks
+    assert int((tp * ks).sum()) == st.particle_steps
+    assert ks.min() >= 1 and ks.max() <= (1 if one_at_a_time else max_steps_per_tick or 16)
     assert (np.diff(t0) >= 0).all() and (t0 >= 0).all()
     if tick_particles:
         sizes = [len(p["mass"]) for p, _, _, _ in reqs]
         assert int(tp.max()) <= max(tick_particles, max(sizes))
     sv.close()
-    return results, st, lat
+    return results, st, lat, ks
 
 
 def test_each_result_is_the_same_alone_and_in_the_mix():
     solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
     reqs = _requests()
-    mixed, st, lat = _serve(solver, reqs, stagger=0.002)
+    mixed, st, lat, _ = _serve(solver, reqs, stagger=0.002)
     assert st.completed == len(reqs) and st.failed == 0 and st.rejected == 0
     assert st.ticks >= max(r[2] for r in reqs)
     assert len(lat) == st.ticks
@@ -69,7 +71,7 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
             assert (got[f] == ref[f]).all(), f
         if mesh:
             assert len(tris) == len(rtris) and (tris == rtris).all()
-    serial, st1, _ = _serve(solver, reqs, one_at_a_time=True)
+    serial, st1, _, _ = _serve(solver, reqs, one_at_a_time=True)
     assert st1.ticks == sum(r[2] for r in reqs)
     for (got, tris), (got1, tris1) in zip(mixed, serial):
         assert (got["position"] == got1["position"]).all()
@@ -81,13 +83,34 @@ def test_tick_groups_bound_the_work_per_tick_and_keep_results():
     # share groups; every result still equals the scene advanced alone
     solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
     reqs = _requests()
-    grouped, st, lat = _serve(solver, reqs, stagger=0.002, tick_particles=32000)
+    grouped, st, lat, _ = _serve(solver, reqs, stagger=0.002, tick_particles=32000)
     assert st.completed == len(reqs) and st.failed == 0
     sizes = [len(p["mass"]) for p, _, _, _ in reqs]
     work = sum(n * steps for n, (_, _, steps, _) in zip(sizes, reqs))
     assert st.particle_steps == work
     assert st.ticks >= work / max(32000, max(sizes))
     for (parts, cfg, steps, mesh), (got, tris) in zip(reqs, grouped):
+        ref, rtris = _alone(solver, parts, cfg, steps, mesh)
+        for f in ("id", "position", "velocity", "colour"):
+            assert (got[f] == ref[f]).all(), f
+        if mesh:
+            assert len(tris) == len(rtris) and (tris == rtris).all()
+    solver.close()
+
+
+def test_small_groups_take_several_steps_a_tick_and_keep_results():
+    # a 400 000-particle tick budget: groups far below half of it advance several
+    # steps per tick (at most 4 here), never past a scene's last step; every result
+    # equals the scene advanced alone and the particle-steps add up
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    reqs = _requests()
+    res, st, lat, ks = _serve(solver, reqs, stagger=0.002, tick_particles=400000, max_steps_per_tick=4)
+    assert st.completed == len(reqs) and st.failed == 0
+    sizes = [len(p["mass"]) for p, _, _, _ in reqs]
+    assert st.particle_steps == sum(n * steps for n, (_, _, steps, _) in zip(sizes, reqs))
+    assert ks.max() > 1
+    assert st.ticks < sum(r[2] for r in reqs)
+    for (parts, cfg, steps, mesh), (got, tris) in zip(reqs, res):
         ref, rtris = _alone(solver, parts, cfg, steps, mesh)
         for f in ("id", "position", "velocity", "colour"):
             assert (got[f] == ref[f]).all(), f
@@ -125,7 +148,7 @@ def test_groups_spread_evenly_and_scenes_move_between_batches():
                                     (8000, 10), (4096, 6)]):
         parts, cfg = scenes.cube_scene(n, 800 + i)
         reqs.append((parts, cfg, steps, False))
-    res, st, lat = _serve(solver, reqs, stagger=0.001, tick_particles=30000)
+    res, st, lat, _ = _serve(solver, reqs, stagger=0.001, tick_particles=30000)
     assert st.completed == len(reqs) and st.failed == 0
     assert st.rebuilds > 0
     for (parts, cfg, steps, _), (got, _) in zip(reqs, res):

@@ -1,11 +1,14 @@
 """Scene sharding across ranks: the assignment, the serving router, and a
-world_size-2 gloo run in which each rank steps its own scenes with the oracle and
-only checksums are exchanged at the end (the GPU path shards the same way)."""
+world_size-2 gloo run of the host path bench.py's sharded legs take
+(partition.sharded_run and combine for the batched leg, route_stream for the
+serving leg) in which each rank steps its own scenes with the oracle and only
+summaries are exchanged at the end."""
 import hashlib
 import json
 import multiprocessing as mp
 import os
 import socket
+import time
 
 import numpy as np
 import pytest
@@ -78,18 +81,43 @@ def test_gather_summary_without_process_group():
     assert partition.gather_summary({"x": 1}) == [{"x": 1}]
 
 
+def test_combine_and_route_stream_single_rank():
+    per_rank = [{"w": 2, "t": 1.5, "d": {0: "a"}, "l": [1]}, {"w": 3, "t": 0.5, "d": {3: "b"}, "l": [2, 3]}]
+    c = partition.combine(per_rank, sum_keys=("w",), max_keys=("t",), merge_keys=("d",), concat_keys=("l",))
+    assert c == {"ranks": 2, "w": 5, "t": 1.5, "d": {0: "a", 3: "b"}, "l": [1, 2, 3]}
+    stream = [(0.0, 100, 10), (0.1, 50, 10), (0.2, 400, 1), (0.3, 10, 10)]
+    assert partition.route_stream(stream, 0, 1) == list(enumerate(stream))
+    r0, r1 = partition.route_stream(stream, 0, 2), partition.route_stream(stream, 1, 2)
+    # particle-steps 1000, 500, 400, 100: the first to rank 0, the rest fill rank 1 up to 1000
+    assert [k for k, _ in r0] == [0] and [k for k, _ in r1] == [1, 2, 3]
+
+
+def _run_local(mine):
+    """A rank's share of the batch, as bench.py's batched leg runs it but with the
+    oracle for the GPU: results by global scene index, work done, time taken."""
+    t0 = time.perf_counter()
+    digests = _step_all(mine)
+    return {"digests": digests, "particles": sum(len(p["mass"]) for _, (p, _) in mine),
+            "seconds": time.perf_counter() - t0}
+
+
 def _worker(rank, world, port, out_path):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        specs = _specs()
-        mine = partition.local_scenes(specs, rank, world)
-        digests = _step_all(mine)
-        everything = partition.gather_summary({"rank": rank, "scenes": [i for i, _ in mine], "digests": digests})
+        # the batched leg's host path: sharded_run, then combine on every rank
+        per_rank = partition.sharded_run(_specs(), rank, world, _run_local)
+        combined = partition.combine(per_rank, sum_keys=("particles",), max_keys=("seconds",),
+                                     merge_keys=("digests",))
+        # the serving leg's host path: a replicated router over the same stream
+        stream = scenes.serving_stream(40, 1.0, seed=3)
+        routed = partition.gather_summary([k for k, _ in partition.route_stream(stream, rank, world)])
         if rank == 0:
             with open(out_path, "w") as f:
-                json.dump(everything, f)
+                json.dump({"ranks": [{"rank": r["rank"], "scenes": r["scenes"]} for r in per_rank],
+                           "digests": combined["digests"], "particles": combined["particles"],
+                           "seconds": combined["seconds"], "routed": routed}, f)
     finally:
         dist.destroy_process_group()
 
@@ -114,11 +142,21 @@ def test_two_rank_sharded_batch_matches_single_process(tmp_path):
         p.join(180)
     assert all(p.exitcode == 0 for p in procs), [p.exitcode for p in procs]
     with open(out) as f:
-        ranks = json.load(f)
+        got = json.load(f)
+    ranks = got["ranks"]
     assert [r["rank"] for r in ranks] == [0, 1]
     owned = sorted(i for r in ranks for i in r["scenes"])
     assert owned == list(range(len(SCENE_TARGETS)))
     assert all(r["scenes"] for r in ranks)  # both ranks got work
-    sharded = {int(k): v for r in ranks for k, v in r["digests"].items()}
-    single = _step_all(list(enumerate(_specs())))
+    specs = _specs()
+    assert got["particles"] == sum(len(p["mass"]) for p, _ in specs)
+    assert got["seconds"] > 0
+    sharded = {int(k): v for k, v in got["digests"].items()}
+    single = _step_all(list(enumerate(specs)))
     assert sharded == single
+    # every request served by exactly one rank, as a single process routes them
+    stream = scenes.serving_stream(40, 1.0, seed=3)
+    routed = got["routed"]
+    assert sorted(k for r in routed for k in r) == list(range(40))
+    assert routed == [[k for k, _ in partition.route_stream(stream, r, 2)] for r in range(2)]
+    assert all(routed)
