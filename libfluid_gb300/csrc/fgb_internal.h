@@ -70,10 +70,7 @@ struct StepView {
     float skin;            // a list stays exact while disp_a + max disp_b <= skin
     float4 *ps_grid;       // p* at grid build (displacements are measured from it)
     float *disp;           // |p - p_grid| per particle after the last delta pass
-    float *dstep;          // distance moved by the last delta pass, per particle
-    // per cell (same index as cells), float bits: {max disp, max dstep} of the last
-    // delta pass over the cell's particles
-    uint2 *cellmax;
+    uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
     // per-pass hit lists: the candidates of one pass that lie within h (and not on top
     // of the particle), in walk order; written by a lambda / vorticity pass, read by the
@@ -81,12 +78,9 @@ struct StepView {
     uint32_t *hlist;       // n * hcap
     uint16_t *hcount;      // entries per particle (kListOverflow: use nlist / the cells)
     uint32_t hcap;
-    // near rows: a hit row that keeps every candidate within h + near_skin of the
-    // positions of the pass that wrote it; near[a] = 1 while particle a's row is such
-    // a row, and slack[a] bounds how far a and its candidates have moved since
-    // (null: near rows off)
+    // near rows: the build pass's hit row keeps every candidate within h + near_skin;
+    // near[a] = 1 while particle a's row is that row (null: near rows off)
     uint8_t *near;
-    float *slack;
     float near_r2;         // (h + near_skin)^2, rounded up
     float near_skin;
     // the step's last kernel also stores each particle's final position and velocity

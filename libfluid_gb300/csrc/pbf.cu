@@ -158,14 +158,12 @@ struct GatherArgs {
     float list_r2, skin;
     const float4 *ps_grid;
     float *disp;
-    float *dstep;
-    uint2 *cellmax;
+    uint32_t *cellmax;
     uint8_t *valid;
     uint32_t *hlist;
     uint16_t *hcount;
     uint32_t hcap;
     uint8_t *near;  // null: no near rows
-    float *slack;
     float near_r2, near_skin;
     uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
     uint32_t *near_stats;  // null, or warps of checked passes on near rows [0] / filtering [1]
@@ -177,16 +175,14 @@ struct GatherArgs {
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
 
-// The largest displacements over the 27 cells around a's cell: {since the grid was
-// built, in the last delta pass}.
-__device__ __forceinline__ float2 max_cell_disp(const SceneDev &S, const uint2 *__restrict__ cellmax,
-                                                uint32_t key, uint32_t mbits) {
+__device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t *__restrict__ cellmax,
+                                               uint32_t key, uint32_t mbits) {
     const uint32_t m = morton_of(key, mbits);
     const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
     const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
-    const uint2 *tbl = cellmax + S.table_base;
+    const uint32_t *tbl = cellmax + S.table_base;
     const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
-    uint32_t best = 0, best_step = 0;  // non-negative floats order like their bit patterns
+    uint32_t best = 0;  // non-negative floats order like their bit patterns
     for (int dz = -1; dz <= 1; ++dz) {
         const int z = cz + dz;
         if (z < 0 || z > ez) continue;
@@ -194,28 +190,23 @@ __device__ __forceinline__ float2 max_cell_disp(const SceneDev &S, const uint2 *
             const int y = cy + dy;
             if (y < 0 || y > ey) continue;
             const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-            for (int x = x0; x <= x1; ++x) {
-                const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                best = max(best, c.x);
-                best_step = max(best_step, c.y);
-            }
+            for (int x = x0; x <= x1; ++x) best = max(best, __ldg(&tbl[spread10((uint32_t)x) | yz]));
         }
     }
-    return make_float2(__uint_as_float(best), __uint_as_float(best_step));
+    return __uint_as_float(best);
 }
 
 // Whether particle a may use its list for the current positions.
-// mcd: the 27 cells' maximum displacement since the grid was built when the caller
-// already has it, else < 0 (then computed here and returned through it).
+// mcd: the 27 cells' maximum displacement when the caller already has it, else < 0.
 template <int MODE>
 __device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
-                                         float &mcd) {
+                                         float mcd = -1.f) {
     if (A.cap == 0 || MODE == kBuild) return false;
     const uint16_t c = A.ncount[a];
     if (c == kListOverflow) return false;
     if (MODE == kFresh) return true;
     if (MODE == kStored) return A.valid[a] != 0;
-    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits).x;
+    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
     const bool ok = A.disp[a] + mcd <= A.skin;
     A.valid[a] = ok ? 1 : 0;
     return ok;
@@ -546,22 +537,16 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
 // walk.  A row that overflows (count > hcap) sends its passes back to the candidates.
 // Rows are particle-major like the Verlet lists.
 //
-// Near rows.  A lambda pass that filters its candidates keeps in the hit row every
-// candidate within h + near_skin of that pass's positions rather than within h, and
-// marks the row (near[a]) with slack[a] = 0.  The row still holds every neighbour
-// within h while the distance a and any candidate have moved since, added up over the
-// passes in between, stays within near_skin: each delta pass records the distance
-// every particle moved (dstep) and its per-cell maximum, and each later pass adds
-// dstep_a + the largest dstep of the 27 cells to slack[a].  A later lambda pass whose
-// warp's rows all hold runs its arithmetic straight over them, without the
-// range-filter phase, and leaves them for the delta pass after it; the vorticity pass
-// likewise.  The extra entries (~15% at 0.05 h) fail the passes' own range tests, so
-// the sums are unchanged.  A warp for which the bound fails on any lane filters
-// again and writes fresh near rows at its current positions -- from a walk, or from
-// a Verlet list whose own bound leaves near_skin of its skin (else the row holds that
-// pass's hits within h and loses the mark).  Bounding the motion per pass rather than
-// since the grid was built keeps rows usable deep into a violent flow, where some
-// particle in nearly every neighbourhood has moved far since the step began.
+// Near rows.  The build pass (the step's first lambda pass) keeps in the hit row
+// every candidate within h + near_skin of the grid positions rather than within h,
+// and marks the row (near[a]).  By the same bound as the Verlet lists, that row still
+// holds every neighbour within h while disp_a + max disp_b <= near_skin, so a later
+// lambda pass for which the bound holds runs its arithmetic straight over the row,
+// without the range-filter phase, and leaves the row for the delta pass after it.
+// The extra entries (~15% at 0.05 h) fail the passes' own range tests, so the sums
+// are unchanged.  A pass for which the bound fails (for any lane of the warp) filters
+// as before and clears the mark: the row it writes holds the hits of that pass's
+// positions only.
 struct RowWriter {
     uint4 *row;
     uint32_t cap, count = 0;
@@ -719,19 +704,14 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     bool done = false;
     if (MODE == kCheck && A.near) {
         bool ok = false;
-        float slack = 0.f;
         if (A.near[a] && have_hits(A, a)) {
-            const float2 m = max_cell_disp(S, A.cellmax, key, A.mbits);
-            mcd = m.x;
-            slack = A.slack[a] + (A.dstep[a] + m.y);
-            ok = slack <= A.near_skin;
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+            ok = A.disp[a] + mcd <= A.near_skin;
         }
         done = __all_sync(__activemask(), ok);
         count_near(A, done);
-        if (done) {
-            A.slack[a] = slack;
-            for_hits(A, a, sp, body);
-        }
+        if (done) for_hits(A, a, sp, body);
+        else A.near[a] = 0;
     }
     if (!done) {
         bool list = use_list<MODE>(A, S, a, key, mcd);
@@ -747,11 +727,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
             // phase 1: range filter (and the Verlet list on the build pass)
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
-            // the row written here is a near row when its candidates hold every one
-            // within h + near_skin: a walk, a fresh list, or a checked list whose bound
-            // leaves near_skin of its skin
-            const bool near_row =
-                A.near && (MODE == kBuild || MODE == kFresh || !list || A.disp[a] + mcd <= A.skin - A.near_skin);
+            const bool near_row = (MODE == kBuild || MODE == kFresh) && A.near;
             // membership only (the arithmetic re-tests every entry exactly): a contracted
             // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
             const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
@@ -772,10 +748,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
                     if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
                 }
             }
-            if (A.near) {
-                A.near[a] = near_row && A.hcap && hits.count <= A.hcap ? 1 : 0;
-                if (near_row) A.slack[a] = 0.f;
-            }
+            if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
             // phase 2: the kernel arithmetic over the hits, in walk order
             if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
             else for_candidates(A, S, a, key, list, sp, body);
@@ -913,7 +886,6 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         ps_out[a] = pa;
         if (A.cap) A.disp[a] = 0.f;
-        if (A.dstep) A.dstep[a] = 0.f;
         if (PROFILE == kRef && last) store_host_motion(hout, a, x[a], v[a]);
         return;
     }
@@ -962,8 +934,7 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
     if (have_hits(A, a)) {
         for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, body);
     } else {
-        float mcd = -1.f;
-        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key, mcd), sp, [&](uint32_t b, const float4 &pb) {
+        for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
             body(b, pb, [&] { return sp.x(b); });
         });
     }
@@ -1000,13 +971,7 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
         const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);
         A.disp[a] = d;
-        // and the distance moved by this pass, for the near rows' bound
-        const float sx = q[0] - pa.x, sy = q[1] - pa.y, sz = q[2] - pa.z;
-        const float ds = sqrtf(sx * sx + sy * sy + sz * sz);
-        if (A.dstep) A.dstep[a] = ds;
-        uint2 *cm = &A.cellmax[S.table_base + morton_of(key, A.mbits)];
-        atomicMax(&cm->x, __float_as_uint(d));
-        atomicMax(&cm->y, __float_as_uint(ds));
+        atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
     }
     if (last) {
         const float4 xa = x[a];
@@ -1079,9 +1044,8 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp
     if (A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
-            const float2 m = max_cell_disp(S, A.cellmax, key, A.mbits);
-            mcd = m.x;
-            ok = A.slack[a] + (A.dstep[a] + m.y) <= A.near_skin;
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
+            ok = A.disp[a] + mcd <= A.near_skin;
         }
         near = __all_sync(__activemask(), ok);
         count_near(A, near);
@@ -1202,8 +1166,7 @@ __device__ __forceinline__ void apply_body(const GatherArgs &A, const Sp &sp, co
         auto row = [&](uint32_t b, const float4 &pb, auto om_b) { body(b, pb, om_b, fluid_rows); };
         for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, row);
     } else {
-        float mcd = -1.f;
-        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key, mcd), sp, [&](uint32_t b, const float4 &pb) {
+        for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
             body(b, pb, [&] { return sp.x(b); }, false);
         });
     }
@@ -1397,9 +1360,7 @@ GatherArgs gather_args(const StepView &s) {
     A.hcount = s.hcount;
     A.hcap = s.hlist ? s.hcap : 0;
     // near rows need the displacement bound (Verlet lists) and hit rows
-    A.near = s.cap && A.hcap && s.slack && s.dstep ? s.near : nullptr;
-    A.slack = s.slack;
-    A.dstep = s.dstep;
+    A.near = s.cap && A.hcap ? s.near : nullptr;
     A.near_r2 = s.near_r2;
     A.near_skin = s.near_skin;
     A.over = s.over;

@@ -522,8 +522,8 @@ struct fgb_batch {
     Dev<float4> ps_grid;
     Dev<uint32_t> nlist;
     Dev<uint16_t> ncount;
-    Dev<float> disp, dstep, slack;
-    Dev<uint2> cellmax;
+    Dev<float> disp;
+    Dev<uint32_t> cellmax;
     Dev<uint8_t> valid;
     Dev<uint32_t> hlist;
     Dev<uint16_t> hcount;
@@ -636,8 +636,6 @@ struct fgb_batch {
         s.skin = skin;
         s.ps_grid = ps_grid.p;
         s.disp = disp.p;
-        s.dstep = dstep.p;
-        s.slack = slack.p;
         s.cellmax = cellmax.p;
         s.valid = valid.p;
         s.hlist = hlist.p;
@@ -687,7 +685,7 @@ struct fgb_batch {
         mark(k, st);
         if (io_up) FGB_CUDA(cudaStreamWaitEvent(st, io_up, cudaEventWaitExternal), "step: upload event");
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
-        if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint2), st), "step: clear cellmax");
+        if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
         if (ph.profile == FGB_PROFILE_REF) {
@@ -707,7 +705,7 @@ struct fgb_batch {
             // starts from the clear above), so an iteration that overshoots does not keep
             // lists invalid after the next one has moved the particles back
             if (it > 0 && cellmax.p)
-                FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint2), st), "step: clear cellmax");
+                FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
             l += (it == 0 && s.cap) ? 3 : 2;
@@ -1078,11 +1076,7 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
         FGB_CUDA(b->hlist.alloc(cap * b->hit_cap), "batch alloc hit lists");
         FGB_CUDA(b->hcount.alloc(cap), "batch alloc");
     }
-    if (b->list_cap && b->hit_cap) {
-        FGB_CUDA(b->near.alloc(cap), "batch alloc");
-        FGB_CUDA(b->dstep.alloc(cap), "batch alloc");
-        FGB_CUDA(b->slack.alloc(cap), "batch alloc");
-    }
+    if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
     if (b->halo) {
