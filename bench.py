@@ -263,7 +263,6 @@ def bench_batched(params, steps=100, mc_every=10, tune=True, rank=0, world=1):
         batch.sync()
         t_batched = time.perf_counter() - t0
         launches = batch.launches - launches0
-        halo = batch.halo_usage()
         batch.close()
         singles = [Batch(solver, [(scenes.copy_particles(p), c)]) for p, c in local]
         for b in singles:
@@ -303,10 +302,10 @@ def bench_batched(params, steps=100, mc_every=10, tune=True, rank=0, world=1):
             sv.close()
         torch.cuda.synchronize()
         return {"particles": total, "batched_s": t_batched, "loop_s": t_loop, "plain_s": t_plain,
-                "launches": launches, "triangles": tris, "halo_ctas": halo[1], "ctas": halo[0]}
+                "launches": launches, "triangles": tris}
 
     per_rank = partition.sharded_run(specs, rank, world, run_local)
-    r = partition.combine(per_rank, sum_keys=("particles", "launches", "triangles", "halo_ctas", "ctas"),
+    r = partition.combine(per_rank, sum_keys=("particles", "launches", "triangles"),
                           max_keys=("batched_s", "loop_s", "plain_s"))
     total = r["particles"]
     v_b = total * steps / r["batched_s"]
@@ -317,7 +316,6 @@ def bench_batched(params, steps=100, mc_every=10, tune=True, rank=0, world=1):
             "per_scene_loop_particle_steps_per_s": v_l, "speedup": v_b / v_l,
             "per_scene_advance_loop_particle_steps_per_s": v_p, "speedup_vs_advance_loop": v_b / v_p,
             "batched_launches": r["launches"], "triangles": r["triangles"],
-            "halo_ctas_fraction": r["halo_ctas"] / r["ctas"] if r["ctas"] else 0.0,
             "arms": "batched: one resident batch; loop: the same scenes as resident single-scene batches; "
                     "advance loop: one drop-in solver per scene, advance() with host arrays every frame"}
 

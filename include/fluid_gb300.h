@@ -229,11 +229,6 @@ int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
 int fgb_batch_sync(fgb_batch *b);
 /* Device error flags raised by bounded waits since the last call (0: none). */
 int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags);
-/* The shared-memory halo of the gather kernels at the last step: CTAs of the step
- * and how many of them read their neighbours from shared memory (the rest read
- * global memory: their particles span two scenes or their box is too large).  Both
- * 0 when the batch runs without the halo.  Synchronous; changes no result. */
-int fgb_batch_halo_usage(fgb_batch *b, uint32_t *ctas, uint32_t *halo_ctas);
 /* With FGB_ROW_STATS=1 in the environment when the batch is created: warps of the
  * checked neighbour passes (later lambda passes, the vorticity pass) that ran on
  * their near rows and warps that filtered their candidates instead, summed over the

@@ -91,19 +91,8 @@ struct StepView {
     // null, or [0] warps of the checked passes that ran on their near rows and [1]
     // warps that filtered their candidates instead (accumulated until read)
     uint32_t *near_stats;
-    // shared-memory halo of every CTA of halo_threads() particles (pbf.cu; null: off)
-    void *halo_hdr;
-    uint2 *halo_box;
 };
 
-// the shared-memory halo of the gathers (pbf.cu): bytes of its per-step arrays for n
-// particles, the CTA size it needs, and the kernel attributes it sets once per device
-uint64_t halo_header_bytes(uint64_t n);
-uint64_t halo_box_bytes(uint64_t n);
-uint32_t halo_threads();
-// CTAs in halo mode among `ctas` headers copied to the host
-uint32_t halo_count(const void *host_headers, uint64_t ctas);
-cudaError_t halo_setup();
 
 constexpr uint16_t kListOverflow = 0xffffu;
 

@@ -167,10 +167,6 @@ struct GatherArgs {
     float near_r2, near_skin;
     uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
     uint32_t *near_stats;  // null, or warps of checked passes on near rows [0] / filtering [1]
-    // shared-memory halo per CTA of kHaloThreads particles (null: every CTA reads
-    // global memory); the build pass writes them, the later passes of the step read them
-    struct HaloHdr *halo_hdr;
-    uint2 *halo_box;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -212,162 +208,8 @@ __device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S,
     return ok;
 }
 
-// ------------------------------------------------------------------- halo
-//
-// Shared-memory halo.  The gathers' neighbour reads are scattered: each lane reads its
-// own neighbours' 16-byte records, ~20 distinct sectors a warp load, and the L1 data
-// pipe (shared with shared memory) saturates on them.  In halo mode a CTA of
-// kHaloThreads consecutive sorted particles first copies into shared memory, cell run
-// after cell run, the per-particle data its pass reads of neighbours (p* and the
-// pass's second array) for every cell of its box: the bounding box of its particles'
-// cells grown by one cell on every side and cut to the grid.  All 27 neighbour cells
-// of every particle of the CTA lie in the box.  The rows of the step (Verlet, hit and
-// near rows) then hold slots of that copy instead of particle indices, and a walk
-// finds a neighbour cell's slots through the box table.  The step's list-build pass
-// builds each CTA's box and table and writes them out; every later pass of the step
-// runs the same CTAs over the same particles and reads them back.  A CTA whose
-// particles span two scenes, whose box exceeds kHaloBox cells or whose cells hold
-// more than kHaloCap particles reads global memory instead.  Walks and rows keep their
-// order, so every sum is the same either way.
-constexpr uint32_t kHaloThreads = 256;
-constexpr uint32_t kHaloCap = 2048;  // particles a CTA stages
-constexpr uint32_t kHaloBox = 512;   // cells of a CTA's box
-
-struct HaloHdr {
-    int32_t ok;          // 1: the CTA reads its halo from shared memory
-    int32_t x0, y0, z0;  // box origin, cells
-    int32_t bx, by, bz;  // box extent, cells
-    uint32_t vol, parts; // cells in the box, particles staged
-};
-
-// Box table entry: {first particle of the cell, slot of its first particle << 16 |
-// particles in the cell}.
-__device__ __forceinline__ uint32_t box_slot(uint2 e) { return e.y >> 16; }
-__device__ __forceinline__ uint32_t box_count(uint2 e) { return e.y & 0xffffu; }
-
-// Copy the halo's runs into shared memory: one warp per box cell, its particles'
-// records read as one contiguous run.  sex / sty may be null.
-template <class T>
-__device__ __forceinline__ void halo_copy(const uint2 *box, uint32_t vol, const float4 *__restrict__ ps,
-                                          float4 *sps, const T *__restrict__ ex, T *sex,
-                                          const int32_t *__restrict__ type, uint8_t *sty) {
-    const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (uint32_t i = w; i < vol; i += nw) {
-        const uint2 e = box[i];
-        const uint32_t start = e.x, off = box_slot(e), cnt = box_count(e);
-        for (uint32_t k = lane; k < cnt; k += 32) {
-            sps[off + k] = __ldg(&ps[start + k]);
-            if (sex) sex[off + k] = __ldg(&ex[start + k]);
-            if (sty) sty[off + k] = (uint8_t)__ldg(&type[start + k]);
-        }
-    }
-}
-
-// The list-build pass: this CTA's box, its table (counts, then slots by an exclusive
-// scan in box order) and the staged p*.  Every thread of the CTA calls it; returns
-// whether the CTA runs in halo mode.
-__device__ bool halo_build(const GatherArgs &A, const float4 *__restrict__ ps, HaloHdr &h, uint2 *box,
-                           float4 *sps) {
-    __shared__ int s_lo[3], s_hi[3];
-    __shared__ uint32_t s_scene[2], s_warp[kHaloThreads / 32];
-    const uint32_t tid = threadIdx.x, a = blockIdx.x * blockDim.x + tid;
-    if (tid == 0) {
-        for (int d = 0; d < 3; ++d) s_lo[d] = 0x7fffffff, s_hi[d] = -1;
-        s_scene[0] = 0xffffffffu, s_scene[1] = 0u;
-    }
-    __syncthreads();
-    if (a < A.n) {
-        const uint32_t key = A.keys[a], m = morton_of(key, A.mbits), sc = scene_of(key, A.mbits);
-        const int c[3] = {(int)compact10(m), (int)compact10(m >> 1), (int)compact10(m >> 2)};
-        for (int d = 0; d < 3; ++d) atomicMin(&s_lo[d], c[d]), atomicMax(&s_hi[d], c[d]);
-        atomicMin(&s_scene[0], sc);
-        atomicMax(&s_scene[1], sc);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        HaloHdr t{};
-        if (s_scene[0] == s_scene[1]) {
-            const SceneDev &S = A.scenes[s_scene[0]];
-            int lo[3], hi[3];
-            for (int d = 0; d < 3; ++d) {
-                lo[d] = s_lo[d] > 0 ? s_lo[d] - 1 : 0;
-                hi[d] = s_hi[d] < (int)S.ext[d] ? s_hi[d] + 1 : (int)S.ext[d];
-            }
-            t.x0 = lo[0], t.y0 = lo[1], t.z0 = lo[2];
-            t.bx = hi[0] - lo[0] + 1, t.by = hi[1] - lo[1] + 1, t.bz = hi[2] - lo[2] + 1;
-            const uint64_t vol = (uint64_t)t.bx * (uint64_t)t.by * (uint64_t)t.bz;
-            t.ok = vol <= kHaloBox;
-            t.vol = t.ok ? (uint32_t)vol : 0u;
-        }
-        h = t;
-    }
-    __syncthreads();
-    if (h.ok) {
-        const SceneDev &S = A.scenes[s_scene[0]];
-        const uint2 *tbl = A.cells + S.table_base;
-        for (uint32_t i = tid; i < h.vol; i += blockDim.x) {
-            const uint32_t x = (uint32_t)h.x0 + i % (uint32_t)h.bx;
-            const uint32_t y = (uint32_t)h.y0 + (i / (uint32_t)h.bx) % (uint32_t)h.by;
-            const uint32_t z = (uint32_t)h.z0 + i / ((uint32_t)h.bx * (uint32_t)h.by);
-            const uint2 c = __ldg(&tbl[morton3(x, y, z)]);
-            box[i] = make_uint2(c.x, c.y > c.x ? c.y - c.x : 0u);
-        }
-        __syncthreads();
-        // exclusive scan of the counts in box order: two entries a thread
-        const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
-        const uint32_t c0 = i0 < h.vol ? box[i0].y : 0u, c1 = i1 < h.vol ? box[i1].y : 0u;
-        uint32_t x = c0 + c1;
-        const uint32_t lane = tid & 31u, w = tid >> 5;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (uint32_t)o) x += y;
-        }
-        if (lane == 31) s_warp[w] = x;
-        __syncthreads();
-        uint32_t base = 0, total = 0;
-        for (uint32_t k = 0; k < blockDim.x / 32; ++k) {
-            if (k < w) base += s_warp[k];
-            total += s_warp[k];
-        }
-        const uint32_t ex0 = base + x - (c0 + c1);
-        // counts stay below 2^16 and slots below kHaloCap where the CTA stages
-        if (i0 < h.vol) box[i0].y = (min(ex0, 0xffffu) << 16) | min(c0, 0xffffu);
-        if (i1 < h.vol) box[i1].y = (min(ex0 + c0, 0xffffu) << 16) | min(c1, 0xffffu);
-        __syncthreads();
-        if (tid == 0) {
-            h.parts = total;
-            if (total > kHaloCap) h.ok = 0;
-        }
-        __syncthreads();
-    }
-    if (tid == 0) A.halo_hdr[blockIdx.x] = h;
-    if (!h.ok) return false;
-    uint2 *gbox = A.halo_box + (size_t)blockIdx.x * kHaloBox;
-    for (uint32_t i = tid; i < h.vol; i += blockDim.x) gbox[i] = box[i];
-    halo_copy<float>(box, h.vol, ps, sps, nullptr, nullptr, nullptr, nullptr);
-    __syncthreads();
-    return true;
-}
-
-// A later pass of the step: this CTA's box and table as the build pass left them, and
-// the pass's arrays staged.  Every thread of the CTA calls it.
-template <class T>
-__device__ bool halo_load(const GatherArgs &A, HaloHdr &h, uint2 *box, float4 *sps, const float4 *__restrict__ ps,
-                          T *sex, const T *__restrict__ ex, uint8_t *sty) {
-    if (threadIdx.x == 0) h = A.halo_hdr[blockIdx.x];
-    __syncthreads();
-    if (!h.ok) return false;
-    const uint2 *gbox = A.halo_box + (size_t)blockIdx.x * kHaloBox;
-    for (uint32_t i = threadIdx.x; i < h.vol; i += blockDim.x) box[i] = gbox[i];
-    __syncthreads();
-    halo_copy<T>(box, h.vol, ps, sps, ex, sex, A.type, sty);
-    __syncthreads();
-    return true;
-}
-
 // Where a gather finds its neighbours' data.  GlobalSpace: the batch arrays by sorted
-// particle index, walks through the cell table.  HaloSpace: the CTA's shared-memory
-// copy by slot, walks through the box table.  pos(b): p* of candidate b; x(b): the
+// particle index, walks through the cell table.  pos(b): p* of candidate b; x(b): the
 // pass's second array; fluid(b): whether b is not an obstacle.
 constexpr int kPrefetch = 4;
 
@@ -413,39 +255,6 @@ struct GlobalSpace {
             for (int k = 0; k < kPrefetch; ++k) f(b + k, p[k]);
         }
         for (; b < hi; ++b) f(b, pos(b));
-    }
-};
-
-template <class T>
-struct HaloSpace {
-    const float4 *ps;   // shared memory, by slot
-    const T *ex;        // shared memory, by slot
-    const uint8_t *type;
-    const uint2 *box;
-    HaloHdr h;
-    __device__ __forceinline__ float4 pos(uint32_t b) const { return ps[b]; }
-    __device__ __forceinline__ T x(uint32_t b) const { return ex[b]; }
-    __device__ __forceinline__ bool fluid(uint32_t b) const { return type[b] != FGB_TYPE_OBSTACLE; }
-    template <class F>
-    __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f) const {
-        const uint32_t m = morton_of(key, A.mbits);
-        const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
-        const int ex_ = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
-        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex_ ? cx + 1 : ex_;
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int z = cz + dz;
-            if (z < 0 || z > ez) continue;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int y = cy + dy;
-                if (y < 0 || y > ey) continue;
-                const int row = h.bx * ((y - h.y0) + h.by * (z - h.z0)) - h.x0;
-                for (int x = x0; x <= x1; ++x) {
-                    const uint2 e = box[row + x];
-                    const uint32_t lo = box_slot(e);
-                    for (uint32_t b = lo; b < lo + box_count(e); ++b) f(b, ps[b]);
-                }
-            }
-        }
     }
 };
 
@@ -627,23 +436,8 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, const Sp &sp, co
     }
 }
 
-// Shared memory of the halo: the box table, then the staged p*, then the pass's
-// second array (T) and the types, as the pass needs them.
-template <class T, bool kTypes>
-constexpr size_t halo_smem_bytes() {
-    return kHaloBox * sizeof(uint2) + kHaloCap * sizeof(float4) + (sizeof(T) > 1 ? kHaloCap * sizeof(T) : 0) +
-           (kTypes ? kHaloCap : 0);
-}
-
 __global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 *__restrict__ ps) {
-    extern __shared__ uint4 halo_smem[];
-    __shared__ HaloHdr h;
-    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
-    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
-    if (A.halo_hdr && halo_build(A, ps, h, box, sps))
-        build_body(A, HaloSpace<char>{sps, nullptr, nullptr, box, h}, ps);
-    else
-        build_body(A, GlobalSpace<char>{ps, nullptr, A.type}, ps);
+    build_body(A, GlobalSpace<char>{ps, nullptr, A.type}, ps);
 }
 
 template <int PROFILE, int MODE, class Sp>
@@ -775,14 +569,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
 template <int PROFILE, int MODE>
 __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
                                                 float *__restrict__ lambda, float *__restrict__ density) {
-    extern __shared__ uint4 halo_smem[];
-    __shared__ HaloHdr h;
-    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
-    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
-    if (A.halo_hdr && halo_load<char>(A, h, box, sps, ps, nullptr, nullptr, nullptr))
-        lambda_body<PROFILE, MODE>(A, HaloSpace<char>{sps, nullptr, nullptr, box, h}, ps, lambda, density);
-    else
-        lambda_body<PROFILE, MODE>(A, GlobalSpace<char>{ps, nullptr, A.type}, ps, lambda, density);
+    lambda_body<PROFILE, MODE>(A, GlobalSpace<char>{ps, nullptr, A.type}, ps, lambda, density);
 }
 
 __device__ __forceinline__ float corr_pow(float ratio, float n) {
@@ -999,17 +786,8 @@ __global__ void __launch_bounds__(256)
     k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
             float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
             const HostParticlesOut *__restrict__ hout) {
-    extern __shared__ uint4 halo_smem[];
-    __shared__ HaloHdr h;
-    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
-    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
-    float *slam = reinterpret_cast<float *>(sps + kHaloCap);
-    if (A.halo_hdr && halo_load<float>(A, h, box, sps, ps_in, slam, lambda, nullptr))
-        delta_body<PROFILE, MODE>(A, HaloSpace<float>{sps, slam, nullptr, box, h}, ps_in, lambda, ps_out, x, v,
-                                  last, hout);
-    else
-        delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
-                                  hout);
+    delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
+                              hout);
 }
 
 __device__ __forceinline__ void cross3(const float *a, const float *b, float *o) {
@@ -1115,16 +893,7 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp
 __global__ void __launch_bounds__(256)
     k_vorticity_xsph(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ v,
                      float4 *__restrict__ omega, float4 *__restrict__ vx) {
-    extern __shared__ uint4 halo_smem[];
-    __shared__ HaloHdr h;
-    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
-    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
-    float4 *sv = sps + kHaloCap;
-    uint8_t *sty = reinterpret_cast<uint8_t *>(sv + kHaloCap);
-    if (A.halo_hdr && halo_load<float4>(A, h, box, sps, ps, sv, v, sty))
-        vorticity_body(A, HaloSpace<float4>{sps, sv, sty, box, h}, ps, v, omega, vx);
-    else
-        vorticity_body(A, GlobalSpace<float4>{ps, v, A.type}, ps, v, omega, vx);
+    vorticity_body(A, GlobalSpace<float4>{ps, v, A.type}, ps, v, omega, vx);
 }
 
 // Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
@@ -1197,16 +966,7 @@ __global__ void __launch_bounds__(256)
     k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
                       const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
                       const HostParticlesOut *__restrict__ hout) {
-    extern __shared__ uint4 halo_smem[];
-    __shared__ HaloHdr h;
-    uint2 *box = reinterpret_cast<uint2 *>(halo_smem);
-    float4 *sps = reinterpret_cast<float4 *>(box + kHaloBox);
-    float4 *som = sps + kHaloCap;
-    uint8_t *sty = reinterpret_cast<uint8_t *>(som + kHaloCap);
-    if (A.halo_hdr && halo_load<float4>(A, h, box, sps, ps, som, omega, sty))
-        apply_body(A, HaloSpace<float4>{sps, som, sty, box, h}, ps, omega, vx, v, x, hout);
-    else
-        apply_body(A, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
+    apply_body(A, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
 }
 
 // Colour diffusion of the ref profile (oclsph_kernel.h:281-303): each fluid particle
@@ -1365,18 +1125,9 @@ GatherArgs gather_args(const StepView &s) {
     A.near_skin = s.near_skin;
     A.over = s.over;
     A.near_stats = A.near ? s.near_stats : nullptr;
-    // the halo needs the list-build pass (which builds it) and CTAs of kHaloThreads
-    const bool halo = s.halo_hdr && s.halo_box && s.cap && s.block == (int)kHaloThreads;
-    A.halo_hdr = halo ? reinterpret_cast<HaloHdr *>(s.halo_hdr) : nullptr;
-    A.halo_box = halo ? s.halo_box : nullptr;
     return A;
 }
 
-// dynamic shared memory of a gather launch: the halo's, or none without it
-template <class T, bool kTypes>
-size_t smem_of(const GatherArgs &A) {
-    return A.halo_hdr ? halo_smem_bytes<T, kTypes>() : 0;
-}
 
 }  // namespace
 
@@ -1422,17 +1173,16 @@ void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStrea
     const GatherArgs A = gather_args(s);
     const unsigned g = grid_for(s.n, s.block);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
-    const size_t sm = smem_of<char, false>(A);
     if (iteration == 0 && A.cap) {
-        k_build_lists<<<g, s.block, sm, st>>>(A, ps);
-        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        k_build_lists<<<g, s.block, 0, st>>>(A, ps);
+        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
     } else if (iteration == 0) {
-        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
     } else {
-        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, sm, st>>>(A, ps, s.lambda, s.density);
+        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
     }
 }
 
@@ -1442,43 +1192,21 @@ void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int it
     const unsigned g = grid_for(s.n, s.block);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
     const int l = last ? 1 : 0;
-    const size_t sm = smem_of<float, false>(A);
     if (iteration == 0) {
-        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     } else {
-        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, sm, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     }
 }
 
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {
     const GatherArgs A = gather_args(s);
     const unsigned g = grid_for(s.n, s.block);
-    const size_t sm = smem_of<float4, true>(A);
-    k_vorticity_xsph<<<g, s.block, sm, st>>>(A, ps, s.v1, s.omega, s.vx);
+    k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
     if (between) between();
-    k_vorticity_apply<<<g, s.block, sm, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
-}
-
-uint64_t halo_header_bytes(uint64_t n) { return ((n + kHaloThreads - 1) / kHaloThreads) * sizeof(HaloHdr); }
-uint64_t halo_box_bytes(uint64_t n) { return ((n + kHaloThreads - 1) / kHaloThreads) * kHaloBox * sizeof(uint2); }
-uint32_t halo_threads() { return kHaloThreads; }
-
-uint32_t halo_count(const void *host_headers, uint64_t ctas) {
-    const HaloHdr *h = static_cast<const HaloHdr *>(host_headers);
-    uint32_t k = 0;
-    for (uint64_t i = 0; i < ctas; ++i) k += h[i].ok ? 1u : 0u;
-    return k;
-}
-
-// The gather kernels' dynamic shared memory above the default 48 KB (the vorticity
-// passes stage two float4 arrays); set once per device, before any graph capture.
-cudaError_t halo_setup() {
-    const int big = (int)halo_smem_bytes<float4, true>();
-    cudaError_t e = cudaFuncSetAttribute(k_vorticity_xsph, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_vorticity_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    return e;
+    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

@@ -277,10 +277,7 @@ std::once_flag g_tables_once[64];
 void ensure_tables() {
     int dev = 0;
     cudaGetDevice(&dev);
-    std::call_once(g_tables_once[dev & 63], [] {
-        mc_tables_upload();
-        halo_setup();
-    });
+    std::call_once(g_tables_once[dev & 63], [] { mc_tables_upload(); });
 }
 
 }  // namespace
@@ -533,11 +530,6 @@ struct fgb_batch {
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
     int block = 128;  // threads per CTA of the gather kernels
-    // the gathers' shared-memory halo (pbf.cu): per-CTA boxes of the step, built by the
-    // list-build pass; needs the Verlet lists and CTAs of halo_threads() particles
-    bool halo = false;
-    Dev<char> halo_hdr, halo_box;
-    uint64_t steps_done = 0;
     Dev<float> lambda, density;
     Dev<float4> omega, vx;
     Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
@@ -650,8 +642,6 @@ struct fgb_batch {
         s.hout = advance_io ? hout_dev.p : nullptr;
         s.over = over.p;
         s.near_stats = row_stats && over.p ? over.p + 2 : nullptr;
-        s.halo_hdr = halo ? (void *)halo_hdr.p : nullptr;
-        s.halo_box = halo ? (uint2 *)halo_box.p : nullptr;
         return s;
     }
 
@@ -759,7 +749,6 @@ struct fgb_batch {
         float best_skin = skin_frac, best_ms = 3.4e38f, ms = 0.f;
         const float skin0 = skin_frac;
         for (int blk : {64, 128, 256}) {
-            if (halo && blk != (int)halo_threads()) continue;  // the halo fixes the CTA size
             rc = trial(blk, skin0, &ms);
             if (rc) break;
             if (ms < best_ms) best_ms = ms, best_block = blk;
@@ -910,7 +899,6 @@ struct fgb_batch {
             FGB_CUDA(cudaGraphLaunch(graph[cur], stream()), "graph launch");
             cur ^= 1;
             launches += launches_per_step;
-            steps_done++;
         }
         if (steps) query_ok = true;
         return FGB_OK;
@@ -1079,10 +1067,6 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
-    if (b->halo) {
-        FGB_CUDA(b->halo_hdr.alloc(halo_header_bytes(cap)), "batch alloc halo");
-        FGB_CUDA(b->halo_box.alloc(halo_box_bytes(cap)), "batch alloc halo");
-    }
     if (p.profile != FGB_PROFILE_REF) {
         FGB_CUDA(b->omega.alloc(cap), "batch alloc");
         FGB_CUDA(b->vx.alloc(cap), "batch alloc");
@@ -1203,13 +1187,6 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_NEAR_SKIN")) b->near_frac = (float)atof(e);
     if (b->hit_cap > 4096) b->hit_cap = 4096;
     b->hit_cap = (b->hit_cap + 3u) & ~3u;  // rows move as 16-byte vectors
-    {
-        // "1": the gathers read their neighbours from a shared-memory halo (pbf.cu);
-        // off by default, as it measured slower than reads through L1
-        const char *e = getenv("FGB_HALO");
-        b->halo = b->list_cap && e && strcmp(e, "1") == 0;
-        if (b->halo) b->block = (int)halo_threads();
-    }
     int rc = alloc_step_arrays(b, n);
     if (rc) return rc;
     FGB_CUDA(b->err.alloc(1), "batch alloc");
@@ -1866,20 +1843,6 @@ int fgb_batch_row_stats(fgb_batch *b, uint32_t *near_warps, uint32_t *filter_war
     FGB_CUDA(cudaStreamSynchronize(st), "row_stats");
     *near_warps = h[0];
     *filter_warps = h[1];
-    return FGB_OK;
-}
-
-int fgb_batch_halo_usage(fgb_batch *b, uint32_t *ctas, uint32_t *halo_ctas) {
-    if (!b || !ctas || !halo_ctas) return fail(FGB_ERR_INVALID, "halo_usage: bad argument");
-    *ctas = *halo_ctas = 0;
-    if (!b->halo || !b->halo_hdr.p || b->n == 0 || b->steps_done == 0) return FGB_OK;
-    const uint64_t n_ctas = (b->n + halo_threads() - 1) / halo_threads();
-    std::vector<char> host(halo_header_bytes(b->n));
-    cudaStream_t st = b->stream();
-    FGB_CUDA(cudaMemcpyAsync(host.data(), b->halo_hdr.p, host.size(), cudaMemcpyDeviceToHost, st), "halo_usage");
-    FGB_CUDA(cudaStreamSynchronize(st), "halo_usage");
-    *ctas = (uint32_t)n_ctas;
-    *halo_ctas = halo_count(host.data(), n_ctas);
     return FGB_OK;
 }
 

@@ -244,12 +244,6 @@ class Batch:
         capi.check(self.lib.fgb_batch_error_flags(self._h, ctypes.byref(f)))
         return int(f.value)
 
-    def halo_usage(self):
-        """(CTAs of the last step, CTAs that read neighbours from shared memory)."""
-        c, h = ctypes.c_uint32(), ctypes.c_uint32()
-        capi.check(self.lib.fgb_batch_halo_usage(self._h, ctypes.byref(c), ctypes.byref(h)))
-        return int(c.value), int(h.value)
-
     def row_stats(self):
         """(warps of checked passes on near rows, warps that filtered) since the last
         call; zeros unless FGB_ROW_STATS=1 was set when the batch was created."""
