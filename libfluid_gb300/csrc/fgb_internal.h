@@ -58,6 +58,10 @@ struct StepView {
     uint64_t cells_n;
     float4 *ps_a, *ps_b;
     float *lambda, *density;
+    // the lambda pass's p* with lambda in w (the delta pass's neighbour reads; null: off)
+    float4 *plam;
+    // {smallest mass, ~largest mass} as float bits, set by the grid build of each step
+    uint32_t *mass_range;
     float4 *omega, *vx;
     uint32_t *err;
     int block;             // threads per CTA of the gather kernels

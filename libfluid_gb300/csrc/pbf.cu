@@ -104,7 +104,13 @@ __global__ void k_reorder_cells(const SceneDev *__restrict__ scenes, const WellD
                                 float4 *__restrict__ x1, float4 *__restrict__ v1, int32_t *__restrict__ type1,
                                 uint32_t *__restrict__ col1, uint32_t *__restrict__ slot1,
                                 float4 *__restrict__ ps, uint2 *__restrict__ cells, uint64_t cells_n,
-                                uint32_t *err) {
+                                uint32_t *err, uint32_t *mass_range) {
+    // the smallest mass's bits and the complement of the largest's, both by atomicMin
+    // (one pair per CTA); the masses are all equal when range[0] == ~range[1]
+    __shared__ uint32_t s_lo, s_hi;
+    if (threadIdx.x == 0) s_lo = s_hi = 0xffffffffu;
+    __syncthreads();
+    uint32_t lo = 0xffffffffu, hi = 0xffffffffu;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t j = vals[i];
         const uint32_t key = keys[i];
@@ -119,6 +125,8 @@ __global__ void k_reorder_cells(const SceneDev *__restrict__ scenes, const WellD
         col1[i] = col0[j];
         slot1[i] = slot0[j];
         ps[i] = make_float4(p.x, p.y, p.z, xj.w);
+        lo = min(lo, __float_as_uint(xj.w));
+        hi = min(hi, ~__float_as_uint(xj.w));
         const uint64_t c = (uint64_t)S.table_base + morton_of(key, mbits);
         if (c >= cells_n) {
             raise_error(err, ERR_CELL_RANGE);
@@ -126,6 +134,17 @@ __global__ void k_reorder_cells(const SceneDev *__restrict__ scenes, const WellD
         }
         if (i == 0 || keys[i - 1] != key) cells[c].x = i;
         if (i + 1 == n || keys[i + 1] != key) cells[c].y = i + 1;
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_min_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31u) == 0) {
+        atomicMin(&s_lo, lo);
+        atomicMin(&s_hi, hi);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && mass_range) {
+        atomicMin(&mass_range[0], s_lo);
+        atomicMin(&mass_range[1], s_hi);
     }
 }
 
@@ -167,6 +186,10 @@ struct GatherArgs {
     float near_r2, near_skin;
     uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
     uint32_t *near_stats;  // null, or warps of checked passes on near rows [0] / filtering [1]
+    // the lambda pass's p* with lambda in w, read by the delta pass (null: off), and the
+    // batch's smallest and largest mass (float bits) of the step
+    float4 *plam;
+    const uint32_t *mass_range;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -218,9 +241,13 @@ struct GlobalSpace {
     const float4 *ps;
     const T *ex;
     const int32_t *type;
+    static constexpr bool kPacked = false;
     __device__ __forceinline__ float4 pos(uint32_t b) const { return __ldg(&ps[b]); }
     __device__ __forceinline__ T x(uint32_t b) const { return __ldg(&ex[b]); }
     __device__ __forceinline__ bool fluid(uint32_t b) const { return __ldg(&type[b]) != FGB_TYPE_OBSTACLE; }
+    // the delta pass's view of a candidate: its mass and its lambda
+    __device__ __forceinline__ float mass(const float4 &pb) const { return pb.w; }
+    __device__ __forceinline__ float lam(uint32_t b, const float4 &) const { return __ldg(&ex[b]); }
     // Visit the particles of the 27 cells in walk order as f(b, p_b); loads run four
     // candidates ahead of the arithmetic.
     template <class F>
@@ -256,6 +283,18 @@ struct GlobalSpace {
         }
         for (; b < hi; ++b) f(b, pos(b));
     }
+};
+
+// The delta pass's candidates through the lambda pass's copy of p* with each
+// particle's lambda in w (plam): one 16-byte load a neighbour instead of p* and lambda
+// apart.  Their masses are then not in w: the ref profile's delta sum uses none, and
+// the baseline takes this path only when every particle of the batch has the same
+// mass (`m`).
+struct PackedSpace : GlobalSpace<float> {
+    float m;
+    static constexpr bool kPacked = true;
+    __device__ __forceinline__ float mass(const float4 &) const { return m; }
+    __device__ __forceinline__ float lam(uint32_t, const float4 &pb) const { return pb.w; }
 };
 
 // Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
@@ -448,6 +487,10 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         lambda[a] = 0.f;
         density[a] = 0.f;
+        if (A.plam) {
+            const float4 p = ps[a];
+            A.plam[a] = make_float4(p.x, p.y, p.z, 0.f);
+        }
         if (MODE == kBuild && A.cap) A.ncount[a] = 0;
         close_hits_empty(A, a);
         return;
@@ -564,6 +607,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     }
     lambda[a] = lam;
     density[a] = dens;
+    if (A.plam) A.plam[a] = make_float4(pa.x, pa.y, pa.z, lam);
 }
 
 template <int PROFILE, int MODE>
@@ -710,7 +754,7 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
                     const float t = ph.hh - q2;
                     const float corr = -ph.corr_k * corr_pow((t * t * t) * ph.inv_corr_wdq, ph.corr_n);
                     const float hr = ph.h - r;
-                    const float sc = pb.w * ((hr * hr) / r) * (la + lam_b() + corr);
+                    const float sc = sp.mass(pb) * ((hr * hr) / r) * (la + lam_b() + corr);
                     px = __fmaf_rn(sc, dx, px);
                     py = __fmaf_rn(sc, dy, py);
                     pz = __fmaf_rn(sc, dz, pz);
@@ -719,10 +763,15 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
         }
     };
     if (have_hits(A, a)) {
-        for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, body);
+        if constexpr (Sp::kPacked) {
+            auto packed = [&](uint32_t b, const float4 &pb) { body(b, pb, [&] { return pb.w; }); };
+            for_row(A.hlist, A.hcap, a, A.hcount[a], sp, packed);
+        } else {
+            for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, body);
+        }
     } else {
         for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
-            body(b, pb, [&] { return sp.x(b); });
+            body(b, pb, [&] { return sp.lam(b, pb); });
         });
     }
     float world[3];
@@ -786,8 +835,15 @@ __global__ void __launch_bounds__(256)
     k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
             float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
             const HostParticlesOut *__restrict__ hout) {
-    delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
-                              hout);
+    // the packed copy when the sums need no neighbour mass or all masses are equal
+    // (the batch's smallest and largest mass, float bits, from the grid build)
+    const bool packed = A.plam && (PROFILE == kRef || A.mass_range[0] == ~A.mass_range[1]);
+    if (packed)
+        delta_body<PROFILE, MODE>(A, PackedSpace{{A.plam, nullptr, A.type}, __uint_as_float(A.mass_range[0])}, ps_in,
+                                  lambda, ps_out, x, v, last, hout);
+    else
+        delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
+                                  hout);
 }
 
 __device__ __forceinline__ void cross3(const float *a, const float *b, float *o) {
@@ -1125,6 +1181,8 @@ GatherArgs gather_args(const StepView &s) {
     A.near_skin = s.near_skin;
     A.over = s.over;
     A.near_stats = A.near ? s.near_stats : nullptr;
+    A.plam = s.plam;
+    A.mass_range = s.mass_range;
     return A;
 }
 
@@ -1166,7 +1224,7 @@ void launch_reorder_cells(const StepView &s, cudaStream_t st) {
     k_reorder_cells<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.wells, s.ph, s.n, s.mbits, s.keys_sorted,
                                                       s.vals_sorted, s.x0, s.v0, s.type0, s.col0, s.slot0, s.x1,
                                                       s.v1, s.type1, s.col1, s.slot1, s.ps_grid, s.cells, s.cells_n,
-                                                      s.err);
+                                                      s.err, s.mass_range);
 }
 
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st) {

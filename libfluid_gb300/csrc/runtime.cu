@@ -531,6 +531,8 @@ struct fgb_batch {
     Dev<uint8_t> near;
     int block = 128;  // threads per CTA of the gather kernels
     Dev<float> lambda, density;
+    Dev<float4> plam;             // the lambda pass's p* with lambda in w (delta reads)
+    Dev<uint32_t> mass_range;     // {min mass, ~max mass} bits of the step
     Dev<float4> omega, vx;
     Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
     Dev<uint32_t> colour_count;
@@ -614,6 +616,8 @@ struct fgb_batch {
         s.ps_a = ps[0].p;
         s.ps_b = ps[1].p;
         s.lambda = lambda.p;
+        s.plam = plam.p;
+        s.mass_range = mass_range.p;
         s.density = density.p;
         s.omega = omega.p;
         s.vx = vx.p;
@@ -675,6 +679,7 @@ struct fgb_batch {
         mark(k, st);
         if (io_up) FGB_CUDA(cudaStreamWaitEvent(st, io_up, cudaEventWaitExternal), "step: upload event");
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
+        FGB_CUDA(cudaMemsetAsync(mass_range.p, 0xff, 2 * sizeof(uint32_t), st), "step: clear mass range");
         if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
@@ -1066,6 +1071,8 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     }
     if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
+    if (!getenv("FGB_NO_PACKED_DELTA")) FGB_CUDA(b->plam.alloc(cap), "batch alloc");
+    FGB_CUDA(b->mass_range.alloc(2), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
         FGB_CUDA(b->omega.alloc(cap), "batch alloc");
