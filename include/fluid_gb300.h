@@ -180,9 +180,10 @@ void fgb_mesh_free(fgb_mesh *m);
  * step's grid (of the predicted positions), the fluid particles in it and their mean
  * colour before the step's colour diffusion; results only for points whose cell holds
  * fluid, in query order, *n_results of them (results must hold n_queries).  A point
- * outside the grid has no result.  Where the device addresses the records directly
- * (a coherent link) kernels read and write them; elsewhere the host threads pack them.
- * mesh_out as in fgb_advance. */
+ * outside the grid has no result.  Records are written back whole: every byte of a
+ * record outside the described fields (padding) becomes zero.  Where the device
+ * addresses the records directly (a coherent link) kernels read and write them;
+ * elsewhere the host threads pack them.  mesh_out as in fgb_advance. */
 int fgb_advance_records(fgb_solver *s, const fgb_config *cfg, fgb_records *xs,
                         const fgb_triangle *colliders, size_t n_colliders,
                         const fgb_query *queries, size_t n_queries,

@@ -177,6 +177,10 @@ struct HostRecords {
 constexpr uint32_t kMaxRecordStride = 128;  // bytes; the upload stages a tile of records in shared memory
 void launch_pack_records(const HostRecords &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
                          uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st);
+// the step's final sorted state into whole records (every byte not in a described
+// field zero)
+void launch_unpack_records(const HostRecords &out, uint64_t n, const float4 *x, const float4 *v, const int32_t *type,
+                           const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st);
 // the HostParticlesOut of a HostRecords (stride set)
 HostParticlesOut record_fields(const HostRecords &r, bool motion, bool fixed);
 

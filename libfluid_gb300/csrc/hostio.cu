@@ -210,7 +210,62 @@ __global__ void __launch_bounds__(kTile) k_pack_records(HostRecords in, uint64_t
     if ((t & 31) == 0 && obst) atomicAdd(obstacles, obst);
 }
 
+// A download into the caller's array of records, whole records at a time: each CTA
+// builds its tile in shared memory (the described fields from the step's final state,
+// every other byte zero) and stores it as 4-byte words in order, so every warp store
+// covers a contiguous run of the host array.  Storing field by field instead leaves
+// each warp store spread over 32 records, a few bytes in each.
+__global__ void __launch_bounds__(kTile) k_unpack_records(HostRecords out, uint64_t n, const float4 *__restrict__ x,
+                                                         const float4 *__restrict__ v, const int32_t *__restrict__ type,
+                                                         const uint32_t *__restrict__ col,
+                                                         const uint32_t *__restrict__ slot,
+                                                         const uint64_t *__restrict__ ids) {
+    __shared__ uint32_t sw[kTile * (kMaxRecordStride / 4)];
+    const unsigned t = threadIdx.x;
+    const uint32_t words = out.stride / 4;
+    for (uint64_t base = (uint64_t)blockIdx.x * kTile; base < n; base += (uint64_t)gridDim.x * kTile) {
+        const uint32_t m = (uint32_t)(n - base < kTile ? n - base : kTile);
+        for (uint32_t j = t; j < m * words; j += kTile) sw[j] = 0u;
+        __syncthreads();
+        if (t < m) {
+            const uint64_t i = base + t;
+            uint32_t *r = sw + t * words;
+            const float4 xi = x[i], vi = v[i];
+            if (out.off_position >= 0) {
+                uint32_t *q = r + out.off_position / 4;
+                q[0] = __float_as_uint(xi.x);
+                q[1] = __float_as_uint(xi.y);
+                q[2] = __float_as_uint(xi.z);
+            }
+            if (out.off_velocity >= 0) {
+                uint32_t *q = r + out.off_velocity / 4;
+                q[0] = __float_as_uint(vi.x);
+                q[1] = __float_as_uint(vi.y);
+                q[2] = __float_as_uint(vi.z);
+            }
+            if (out.off_mass >= 0) r[out.off_mass / 4] = __float_as_uint(xi.w);
+            if (out.off_type >= 0) r[out.off_type / 4] = (uint32_t)type[i];
+            if (out.off_colour >= 0) r[out.off_colour / 4] = col[i];
+            if (out.off_id >= 0) {
+                const uint32_t sl = slot[i];
+                const uint64_t id = sl < n ? ids[sl] : sl;
+                r[out.off_id / 4] = (uint32_t)id;
+                if (out.id_bytes == 8) r[out.off_id / 4 + 1] = (uint32_t)(id >> 32);
+            }
+        }
+        __syncthreads();
+        uint32_t *dst = (uint32_t *)(out.base + base * out.stride);
+        for (uint32_t j = t; j < m * words; j += kTile) dst[j] = sw[j];
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+void launch_unpack_records(const HostRecords &out, uint64_t n, const float4 *x, const float4 *v, const int32_t *type,
+                           const uint32_t *col, const uint32_t *slot, const uint64_t *ids, cudaStream_t st) {
+    if (n) k_unpack_records<<<grid_of(n), kTile, 0, st>>>(out, n, x, v, type, col, slot, ids);
+}
 
 void launch_pack_records(const HostRecords &in, uint64_t n, float4 *x, float4 *v, int32_t *type, uint32_t *col,
                          uint32_t *slot, uint64_t *ids, uint32_t *obstacles, cudaStream_t st) {

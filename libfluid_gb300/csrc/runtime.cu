@@ -2293,7 +2293,7 @@ static int advance_records_direct(fgb_batch *b, const fgb_config *cfg, const Hos
                                   size_t *n_results, fgb_mesh *mesh_out) {
     int rc = b->sync_tris();  // the scene table before the upload counts obstacles into it
     if (rc) return rc;
-    cudaStream_t st = b->stream(), io = b->io_stream;
+    cudaStream_t st = b->stream();
     const int c = b->cur, next = c ^ 1;
     uint32_t *obstacles = &b->d_scenes.p[0].obstacles;
     // the records are inputs and outputs: their pages are readied, contents kept,
@@ -2308,16 +2308,15 @@ static int advance_records_direct(fgb_batch *b, const fgb_config *cfg, const Hos
     b->ids[0].clear();
     b->ids_stale[0] = 0;
     b->query_ok = false;
-    b->st_hout.p[0] = record_fields(r, true, false);
+    // no field stores from the step's last kernel: the records go back whole below
+    b->st_hout.p[0] = record_fields(r, false, false);
     FGB_CUDA(cudaMemcpyAsync(b->hout_dev.p, b->st_hout.p, sizeof(HostParticlesOut), cudaMemcpyHostToDevice, st),
              "advance: output records");
     rc = b->step(1);
     if (rc) return rc;
-    FGB_CUDA(cudaStreamWaitEvent(io, b->grid_ready, 0), "advance: io wait");
-    launch_unpack_static(record_fields(r, false, true), n, b->ps_grid.p, b->type[next].p, b->col[next].p,
-                         b->slot[next].p, b->ids_dev.p, io);
+    launch_unpack_records(r, n, b->x[next].p, b->v[next].p, b->type[next].p, b->col[next].p, b->slot[next].p,
+                          b->ids_dev.p, st);
     FGB_CUDA(cudaGetLastError(), "advance: download kernel");
-    FGB_CUDA(cudaEventRecord(b->io_done, io), "advance: io event");
     if (n_queries) {
         rc = batch_query(b, 0, queries, n_queries, results, n_results);
         if (rc) return rc;
@@ -2328,7 +2327,6 @@ static int advance_records_direct(fgb_batch *b, const fgb_config *cfg, const Hos
     }
     FGB_CUDA(cudaMemcpyAsync(b->st_count.p, obstacles, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
              "advance: obstacle count");
-    FGB_CUDA(cudaStreamWaitEvent(st, b->io_done, 0), "advance: io join");
     FGB_CUDA(cudaStreamSynchronize(st), "advance: sync");
     b->h_scenes[0].obstacles = b->st_count.p[0];  // the device table has it already
     return advance_flags(b);
@@ -2401,6 +2399,7 @@ int fgb_advance_records(fgb_solver *s, const fgb_config *cfg, fgb_records *xs, c
     parallel_for(n, [&](uint64_t lo, uint64_t hi) {
         for (uint64_t i = lo; i < hi; ++i) {
             char *rec = r.base + i * st;
+            memset(rec, 0, st);  // whole records, as the direct path writes them
             memcpy(rec + r.off_position, &pos[3 * i], 12);
             memcpy(rec + r.off_velocity, &vel[3 * i], 12);
             memcpy(rec + r.off_mass, &mass[i], 4);
