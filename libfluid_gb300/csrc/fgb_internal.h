@@ -62,7 +62,6 @@ struct StepView {
     float4 *plam;
     // {smallest mass, ~largest mass} as float bits, set by the grid build of each step
     uint32_t *mass_range;
-    int one_phase;
     float4 *omega, *vx;
     uint32_t *err;
     int block;             // threads per CTA of the gather kernels

@@ -190,7 +190,6 @@ struct GatherArgs {
     // batch's smallest and largest mass (float bits) of the step
     float4 *plam;
     const uint32_t *mass_range;
-    int one_phase;  // lambda filter passes run the arithmetic on each hit as they find it
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -573,10 +572,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
                 const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
                 const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
                 if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
-                if (r2 <= (near_row ? A.near_r2 : hit_r2)) {
-                    hits.add(b);
-                    if (A.one_phase) body(b, pb);
-                }
+                if (r2 <= (near_row ? A.near_r2 : hit_r2)) hits.add(b);
             });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
@@ -590,12 +586,9 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
                 }
             }
             if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
-            // phase 2: the kernel arithmetic over the hits, in walk order (one phase: done
-            // above, candidate by candidate)
-            if (!A.one_phase) {
-                if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
-                else for_candidates(A, S, a, key, list, sp, body);
-            }
+            // phase 2: the kernel arithmetic over the hits, in walk order
+            if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
+            else for_candidates(A, S, a, key, list, sp, body);
         }
     }
     float dens, lam;
@@ -1189,7 +1182,6 @@ GatherArgs gather_args(const StepView &s) {
     A.over = s.over;
     A.near_stats = A.near ? s.near_stats : nullptr;
     A.plam = s.plam;
-    A.one_phase = s.one_phase;
     A.mass_range = s.mass_range;
     return A;
 }

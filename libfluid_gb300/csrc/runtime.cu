@@ -617,7 +617,6 @@ struct fgb_batch {
         s.ps_b = ps[1].p;
         s.lambda = lambda.p;
         s.plam = plam.p;
-        s.one_phase = getenv("FGB_ONE_PHASE") ? 1 : 0;
         s.mass_range = mass_range.p;
         s.density = density.p;
         s.omega = omega.p;
