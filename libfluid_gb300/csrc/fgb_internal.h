@@ -75,7 +75,6 @@ struct StepView {
     float4 *ps_grid;       // p* at grid build (displacements are measured from it)
     float *disp;           // |p - p_grid| per particle after the last delta pass
     uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
-    uint32_t *reach;       // per occupied cell: the max of cellmax over its 27 cells (null: off)
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
     // per-pass hit lists: the candidates of one pass that lie within h (and not on top
     // of the particle), in walk order; written by a lambda / vorticity pass, read by the
@@ -106,8 +105,6 @@ void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
-// after a delta pass: the 27-cell displacement maximum of every occupied cell
-void launch_reach(const StepView &s, cudaStream_t st);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
                   cudaStream_t st);
 // ref-profile colour diffusion of the sorted colours (col1, in place); agg and count

@@ -178,7 +178,6 @@ struct GatherArgs {
     const float4 *ps_grid;
     float *disp;
     uint32_t *cellmax;
-    const uint32_t *reach;  // null, or max_cell_disp per occupied cell (k_reach)
     uint8_t *valid;
     uint32_t *hlist;
     uint16_t *hcount;
@@ -216,27 +215,6 @@ __device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t
     return __uint_as_float(best);
 }
 
-// The largest displacement over the 27 cells around a's cell: one word written by
-// k_reach after the last delta pass, or the 27 cell maxima themselves.
-__device__ __forceinline__ float reach_of(const GatherArgs &A, const SceneDev &S, uint32_t key) {
-    if (A.reach) return __uint_as_float(__ldg(&A.reach[S.table_base + morton_of(key, A.mbits)]));
-    return max_cell_disp(S, A.cellmax, key, A.mbits);
-}
-
-// Once per delta pass: max_cell_disp of every occupied cell, at the cell's first
-// sorted particle, so that the next pass's list and near-row bounds read one word per
-// particle instead of 27 (the same maximum).
-__global__ void k_reach(const SceneDev *__restrict__ scenes, uint32_t n, uint32_t mbits,
-                        const uint32_t *__restrict__ keys, const uint32_t *__restrict__ cellmax,
-                        uint32_t *__restrict__ reach) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t key = keys[i];
-        if (i > 0 && keys[i - 1] == key) continue;
-        const SceneDev &S = scenes[scene_of(key, mbits)];
-        reach[S.table_base + morton_of(key, mbits)] = __float_as_uint(max_cell_disp(S, cellmax, key, mbits));
-    }
-}
-
 // Whether particle a may use its list for the current positions.
 // mcd: the 27 cells' maximum displacement when the caller already has it, else < 0.
 template <int MODE>
@@ -247,7 +225,7 @@ __device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S,
     if (c == kListOverflow) return false;
     if (MODE == kFresh) return true;
     if (MODE == kStored) return A.valid[a] != 0;
-    if (mcd < 0.f) mcd = reach_of(A, S, key);
+    if (mcd < 0.f) mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
     const bool ok = A.disp[a] + mcd <= A.skin;
     A.valid[a] = ok ? 1 : 0;
     return ok;
@@ -584,7 +562,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     if (MODE == kCheck && A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
-            mcd = reach_of(A, S, key);
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
             ok = A.disp[a] + mcd <= A.near_skin;
         }
         done = __all_sync(__activemask(), ok);
@@ -921,7 +899,7 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp
     if (A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
-            mcd = reach_of(A, S, key);
+            mcd = max_cell_disp(S, A.cellmax, key, A.mbits);
             ok = A.disp[a] + mcd <= A.near_skin;
         }
         near = __all_sync(__activemask(), ok);
@@ -1214,7 +1192,6 @@ GatherArgs gather_args(const StepView &s) {
     A.ps_grid = s.ps_grid;
     A.disp = s.disp;
     A.cellmax = s.cellmax;
-    A.reach = s.reach;
     A.valid = s.valid;
     A.hlist = s.hlist;
     A.hcount = s.hcount;
@@ -1301,10 +1278,6 @@ void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int it
         if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
         else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     }
-}
-
-void launch_reach(const StepView &s, cudaStream_t st) {
-    k_reach<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.n, s.mbits, s.keys_sorted, s.cellmax, s.reach);
 }
 
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {

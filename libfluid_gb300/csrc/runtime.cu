@@ -520,7 +520,7 @@ struct fgb_batch {
     Dev<uint32_t> nlist;
     Dev<uint16_t> ncount;
     Dev<float> disp;
-    Dev<uint32_t> cellmax, cellreach;
+    Dev<uint32_t> cellmax;
     Dev<uint8_t> valid;
     Dev<uint32_t> hlist;
     Dev<uint16_t> hcount;
@@ -633,7 +633,6 @@ struct fgb_batch {
         s.ps_grid = ps_grid.p;
         s.disp = disp.p;
         s.cellmax = cellmax.p;
-        s.reach = cellreach.p;
         s.valid = valid.p;
         s.hlist = hlist.p;
         s.hcount = hcount.p;
@@ -703,12 +702,6 @@ struct fgb_batch {
             if (it > 0 && cellmax.p)
                 FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
-            // the next pass's displacement bounds (the ref profile's last delta pass has
-            // none after it)
-            if (s.cap && s.reach && (it + 1 < iterations || ph.profile != FGB_PROFILE_REF)) {
-                launch_reach(s, st);
-                l += 1;
-            }
             mark(k, st);
             l += (it == 0 && s.cap) ? 3 : 2;
             pin = pout;
@@ -1196,10 +1189,7 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
-    if (b->list_cap) {
-        FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
-        if (!getenv("FGB_NO_REACH")) FGB_CUDA(b->cellreach.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
-    }
+    if (b->list_cap) FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
     if (const char *e = getenv("FGB_HIT_CAP")) b->hit_cap = (uint32_t)atoi(e);
     if (const char *e = getenv("FGB_NEAR_SKIN")) b->near_frac = (float)atof(e);
     if (b->hit_cap > 4096) b->hit_cap = 4096;
