@@ -230,11 +230,14 @@ int fgb_batch_surface_fetch(fgb_batch *b, uint32_t scene, fgb_mesh *mesh_out);
 int fgb_batch_sync(fgb_batch *b);
 /* Device error flags raised by bounded waits since the last call (0: none). */
 int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags);
-/* With FGB_ROW_STATS=1 in the environment when the batch is created: warps of the
- * checked neighbour passes (later lambda passes, the vorticity pass) that ran on
- * their near rows and warps that filtered their candidates instead, summed over the
- * steps since the last call (which clears them); both 0 otherwise.  Synchronous. */
-int fgb_batch_row_stats(fgb_batch *b, uint32_t *near_warps, uint32_t *filter_warps);
+/* With FGB_ROW_STATS=1 in the environment when the batch is created, counters of the
+ * checked neighbour passes (the later lambda passes and the vorticity pass) summed
+ * over the steps since the last call, which clears them: [0] warps that ran on their
+ * near rows, [1] warps that filtered their candidates instead, and among the particles
+ * of later lambda passes that filtered, [2] those whose Verlet list held and [3] those
+ * that walked their 27 cells.  Writes min(n, 4) values, zeros without FGB_ROW_STATS.
+ * Synchronous. */
+int fgb_batch_row_stats(fgb_batch *b, uint32_t *stats, uint32_t n);
 /* Number of kernels this batch launched since creation (for accounting). */
 uint64_t fgb_batch_launch_count(const fgb_batch *b);
 /* Stage timing (replaces the reference's DEBUG-only clutil::Stopwatch phases,

@@ -259,7 +259,7 @@ _SIGS = {
     "fgb_batch_surface_fetch": (ctypes.c_int, [c_void_p, ctypes.c_uint32, P(Mesh)]),
     "fgb_batch_sync": (ctypes.c_int, [c_void_p]),
     "fgb_batch_error_flags": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32)]),
-    "fgb_batch_row_stats": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), P(ctypes.c_uint32)]),
+    "fgb_batch_row_stats": (ctypes.c_int, [c_void_p, P(ctypes.c_uint32), ctypes.c_uint32]),
     "fgb_batch_host_io": (ctypes.c_int, [c_void_p, P(ctypes.c_int)]),
     "fgb_batch_prepare": (ctypes.c_int, [c_void_p]),
     "fgb_batch_launch_count": (ctypes.c_uint64, [c_void_p]),

@@ -185,7 +185,9 @@ struct GatherArgs {
     uint8_t *near;  // null: no near rows
     float near_r2, near_skin;
     uint32_t *over;  // build pass: [0] Verlet rows, [1] hit rows that overflowed (null: not counted)
-    uint32_t *near_stats;  // null, or warps of checked passes on near rows [0] / filtering [1]
+    // null, or: warps of checked passes on near rows [0] / filtering [1]; particles of
+    // filtering later lambda passes on their list [2] / walking [3]
+    uint32_t *near_stats;
     // the lambda pass's p* with lambda in w, read by the delta pass (null: off), and the
     // batch's smallest and largest mass (float bits) of the step
     float4 *plam;
@@ -578,6 +580,14 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
         // candidates within h + skin in walk order); the baseline profile is faster with
         // the choice per lane.
         if constexpr (MODE == kCheck && PROFILE == kRef) list = __all_sync(__activemask(), list);
+        if (MODE == kCheck && A.near_stats) {
+            const unsigned m = __activemask();
+            const unsigned on = __ballot_sync(m, list);
+            if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+                atomicAdd(&A.near_stats[2], (uint32_t)__popc(on));
+                atomicAdd(&A.near_stats[3], (uint32_t)__popc(m & ~on));
+            }
+        }
         if (A.hcap == 0 && MODE != kBuild) {
             for_candidates(A, S, a, key, list, sp, body);
         } else {

@@ -1200,8 +1200,8 @@ static int batch_init(fgb_batch *b) {
     FGB_CUDA(b->st_flags.ensure(1), "batch alloc");
     b->st_flags.p[0] = 0;
     if (b->list_cap || b->hit_cap) {
-        FGB_CUDA(b->over.alloc(4), "batch alloc");
-        FGB_CUDA(cudaMemset(b->over.p, 0, 4 * sizeof(uint32_t)), "batch alloc");
+        FGB_CUDA(b->over.alloc(6), "batch alloc");
+        FGB_CUDA(cudaMemset(b->over.p, 0, 6 * sizeof(uint32_t)), "batch alloc");
         const char *e = getenv("FGB_ROW_STATS");
         b->row_stats = e && strcmp(e, "1") == 0;
         FGB_CUDA(b->st_over.ensure(2), "batch alloc");
@@ -1839,17 +1839,16 @@ int fgb_batch_error_flags(fgb_batch *b, uint32_t *flags) {
     return FGB_OK;
 }
 
-int fgb_batch_row_stats(fgb_batch *b, uint32_t *near_warps, uint32_t *filter_warps) {
-    if (!b || !near_warps || !filter_warps) return fail(FGB_ERR_INVALID, "row_stats: bad argument");
-    *near_warps = *filter_warps = 0;
+int fgb_batch_row_stats(fgb_batch *b, uint32_t *stats, uint32_t n) {
+    if (!b || (n && !stats)) return fail(FGB_ERR_INVALID, "row_stats: bad argument");
+    for (uint32_t k = 0; k < n; ++k) stats[k] = 0;
     if (!b->row_stats || !b->over.p) return FGB_OK;
-    uint32_t h[2] = {0, 0};
+    uint32_t h[4] = {0, 0, 0, 0};
     cudaStream_t st = b->stream();
     FGB_CUDA(cudaMemcpyAsync(h, b->over.p + 2, sizeof(h), cudaMemcpyDeviceToHost, st), "row_stats");
     FGB_CUDA(cudaMemsetAsync(b->over.p + 2, 0, sizeof(h), st), "row_stats");
     FGB_CUDA(cudaStreamSynchronize(st), "row_stats");
-    *near_warps = h[0];
-    *filter_warps = h[1];
+    for (uint32_t k = 0; k < n && k < 4; ++k) stats[k] = h[k];
     return FGB_OK;
 }
 

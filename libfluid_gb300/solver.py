@@ -245,11 +245,12 @@ class Batch:
         return int(f.value)
 
     def row_stats(self):
-        """(warps of checked passes on near rows, warps that filtered) since the last
-        call; zeros unless FGB_ROW_STATS=1 was set when the batch was created."""
-        a, b = ctypes.c_uint32(), ctypes.c_uint32()
-        capi.check(self.lib.fgb_batch_row_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
-        return int(a.value), int(b.value)
+        """(warps of checked passes on near rows, warps that filtered, filtering
+        particles on their Verlet list, walking particles) since the last call; zeros
+        unless FGB_ROW_STATS=1 was set when the batch was created."""
+        out = (ctypes.c_uint32 * 4)()
+        capi.check(self.lib.fgb_batch_row_stats(self._h, out, 4))
+        return tuple(int(x) for x in out)
 
     def set_timing(self, on=True):
         capi.check(self.lib.fgb_batch_set_timing(self._h, 1 if on else 0))
