@@ -463,31 +463,17 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, const Sp &sp, co
     const SceneDev &S = A.scenes[scene_of(key, A.mbits)];
     const float4 pa = ps[a];
     RowWriter built(A.nlist, A.cap, a);
-    // with near rows on, the near row as well (the candidates within h + near_skin,
-    // near_skin <= skin): the first lambda pass then runs its arithmetic straight over
-    // it instead of filtering the fresh list back out of HBM
-    HitWriter hits(A, a);
     // membership only (the passes re-test every entry exactly): a contracted r^2,
     // within ~2e-7 of the sum of squares, against a radius rounded up by 1e-5
     for_candidates(A, S, a, key, false, sp, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-        const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        if (r2 <= A.list_r2) built.add(b);
-        if (A.near && r2 <= A.near_r2) hits.add(b);
+        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
     });
     A.ncount[a] = built.close();
-    if (A.near) {
-        hits.close(A, a);
-        A.near[a] = hits.count <= A.hcap ? 1 : 0;
-    }
     if (A.over) {  // one atomic per warp, when rows overflowed
         const unsigned m = __activemask();
         const unsigned lo = __ballot_sync(m, built.count > A.cap);
-        const unsigned ho = __ballot_sync(m, A.near && hits.count > A.hcap);
-        if ((lo | ho) && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
-            if (lo) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
-            if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
-        }
+        if (lo && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
     }
 }
 
@@ -555,12 +541,6 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     // paths would run both one after the other
     float mcd = -1.f;
     bool done = false;
-    if (MODE == kFresh && A.near) {
-        // the build pass wrote the near rows: the whole warp runs over them unless a
-        // row overflowed
-        done = __all_sync(__activemask(), A.near[a] && have_hits(A, a));
-        if (done) for_hits(A, a, sp, body);
-    }
     if (MODE == kCheck && A.near) {
         bool ok = false;
         if (A.near[a] && have_hits(A, a)) {
@@ -609,8 +589,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
             if ((MODE == kBuild || MODE == kFresh) && A.over) {  // one atomic per warp, when rows overflowed
                 const unsigned m = __activemask();
                 const unsigned lo = __ballot_sync(m, MODE == kBuild && A.cap && built.count > A.cap);
-                // (with near rows the build pass counted the hit rows already)
-                const unsigned ho = __ballot_sync(m, A.hcap && !(MODE == kFresh && A.near) && hits.count > A.hcap);
+                const unsigned ho = __ballot_sync(m, A.hcap && hits.count > A.hcap);
                 if ((lo | ho) && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
                     if (lo) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
                     if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
