@@ -258,6 +258,8 @@ typedef struct fgb_tune_result {
     float skin;          /* Verlet skin, in units of h */
     float ms_per_step;   /* of the chosen shape */
     uint32_t trials, steps;
+    uint32_t persistent; /* 1: the gathers run as persistent grids over a tile queue */
+    uint32_t particles_per_thread;  /* of a persistent grid's tiles (1 otherwise) */
 } fgb_tune_result;
 int fgb_batch_autotune(fgb_batch *b, uint32_t steps_per_trial, fgb_tune_result *out);
 int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count);

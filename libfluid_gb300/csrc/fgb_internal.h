@@ -65,6 +65,12 @@ struct StepView {
     float4 *omega, *vx;
     uint32_t *err;
     int block;             // threads per CTA of the gather kernels
+    // persistent gathers (null: flat grids): one zeroed tile counter per gather launch
+    // of the step (slots_of_step), ppt particles per thread of a tile
+    uint32_t *queue;
+    uint32_t ppt;
+    uint32_t iterations;
+    int sm_count;
     // per-step neighbour lists (Verlet lists with a skin), particle-major rows of cap
     // entries (cap a multiple of 4): list[a * cap + j]
     uint32_t *nlist;       // n * cap candidate indices, in 27-cell walk order
@@ -105,6 +111,8 @@ void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
+// tile counters a step's gather launches use (persistent gathers)
+uint32_t slots_of_step(uint32_t iterations);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
                   cudaStream_t st);
 // ref-profile colour diffusion of the sorted colours (col1, in place); agg and count

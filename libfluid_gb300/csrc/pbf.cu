@@ -192,6 +192,10 @@ struct GatherArgs {
     // batch's smallest and largest mass (float bits) of the step
     float4 *plam;
     const uint32_t *mass_range;
+    // null: one particle per thread over a flat grid; else this launch's tile counter
+    // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
+    uint32_t *queue;
+    uint32_t ppt;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -447,13 +451,39 @@ __device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const 
     for_row(A.hlist, A.hcap, a, A.hcount[a], sp, f);
 }
 
+// The particles of one gather launch, f(a) for each.  Flat: one particle per thread,
+// one CTA per blockDim particles.  Persistent: a grid sized to the GPU whose CTAs take
+// tiles of ppt x blockDim consecutive sorted particles -- a block of cells of one
+// scene, or of a few small ones -- from an atomic counter until none is left, each
+// thread ppt particles of a tile, blockDim apart.  Every particle's work is the same
+// either way.
+template <bool kTiles, class F>
+__device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
+    if constexpr (!kTiles) {
+        f(blockIdx.x * blockDim.x + threadIdx.x);
+        return;
+    }
+    __shared__ uint32_t s_tile;
+    const uint64_t span = (uint64_t)blockDim.x * A.ppt;
+    for (;;) {
+        __syncthreads();  // every thread has read the previous tile
+        if (threadIdx.x == 0) s_tile = atomicAdd(A.queue, 1u);
+        __syncthreads();
+        const uint64_t base = (uint64_t)s_tile * span;
+        if (base >= A.n) break;
+        for (uint32_t k = 0; k < A.ppt; ++k) {
+            const uint64_t a = base + (uint64_t)k * blockDim.x + threadIdx.x;
+            f(a < A.n ? (uint32_t)a : A.n);  // A.n: past the end, the body returns
+        }
+    }
+}
+
 // The step's Verlet lists on their own: each particle walks its 27 cells and keeps, in
 // walk order, every candidate within h + skin.  The first lambda pass then filters the
 // fresh lists (near rows) instead of walking, so the walk carries one row writer and
 // no kernel arithmetic.
 template <class Sp>
-__device__ __forceinline__ void build_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps) {
-    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps) {
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         A.ncount[a] = 0;
@@ -477,14 +507,14 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, const Sp &sp, co
     }
 }
 
+template <bool kTiles>
 __global__ void __launch_bounds__(256) k_build_lists(GatherArgs A, const float4 *__restrict__ ps) {
-    build_body(A, GlobalSpace<char>{ps, nullptr, A.type}, ps);
+    for_tiles<kTiles>(A, [&](uint32_t a) { build_body(A, a, GlobalSpace<char>{ps, nullptr, A.type}, ps); });
 }
 
 template <int PROFILE, int MODE, class Sp>
-__device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+__device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps,
                                             float *__restrict__ lambda, float *__restrict__ density) {
-    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         lambda[a] = 0.f;
@@ -620,10 +650,12 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, const Sp &sp, c
     if (A.plam) A.plam[a] = make_float4(pa.x, pa.y, pa.z, lam);
 }
 
-template <int PROFILE, int MODE>
+template <int PROFILE, int MODE, bool kTiles>
 __global__ void __launch_bounds__(256) k_lambda(GatherArgs A, const float4 *__restrict__ ps,
                                                 float *__restrict__ lambda, float *__restrict__ density) {
-    lambda_body<PROFILE, MODE>(A, GlobalSpace<char>{ps, nullptr, A.type}, ps, lambda, density);
+    for_tiles<kTiles>(A, [&](uint32_t a) {
+        lambda_body<PROFILE, MODE>(A, a, GlobalSpace<char>{ps, nullptr, A.type}, ps, lambda, density);
+    });
 }
 
 __device__ __forceinline__ float corr_pow(float ratio, float n) {
@@ -717,11 +749,10 @@ __device__ __forceinline__ void store_host_motion(const HostParticlesOut *__rest
 }
 
 template <int PROFILE, int MODE, class Sp>
-__device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps_in,
+__device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps_in,
                                            const float *__restrict__ lambda, float4 *__restrict__ ps_out,
                                            float4 *__restrict__ x, float4 *__restrict__ v, int last,
                                            const HostParticlesOut *__restrict__ hout) {
-    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     const float4 pa = ps_in[a];
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
@@ -840,7 +871,7 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, const Sp &sp, co
     }
 }
 
-template <int PROFILE, int MODE>
+template <int PROFILE, int MODE, bool kTiles>
 __global__ void __launch_bounds__(256)
     k_delta(GatherArgs A, const float4 *__restrict__ ps_in, const float *__restrict__ lambda,
             float4 *__restrict__ ps_out, float4 *__restrict__ x, float4 *__restrict__ v, int last,
@@ -848,12 +879,14 @@ __global__ void __launch_bounds__(256)
     // the packed copy when the sums need no neighbour mass or all masses are equal
     // (the batch's smallest and largest mass, float bits, from the grid build)
     const bool packed = A.plam && (PROFILE == kRef || A.mass_range[0] == ~A.mass_range[1]);
-    if (packed)
-        delta_body<PROFILE, MODE>(A, PackedSpace{{A.plam, nullptr, A.type}, __uint_as_float(A.mass_range[0])}, ps_in,
-                                  lambda, ps_out, x, v, last, hout);
-    else
-        delta_body<PROFILE, MODE>(A, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v, last,
-                                  hout);
+    for_tiles<kTiles>(A, [&](uint32_t a) {
+        if (packed)
+            delta_body<PROFILE, MODE>(A, a, PackedSpace{{A.plam, nullptr, A.type}, __uint_as_float(A.mass_range[0])},
+                                      ps_in, lambda, ps_out, x, v, last, hout);
+        else
+            delta_body<PROFILE, MODE>(A, a, GlobalSpace<float>{ps_in, lambda, A.type}, ps_in, lambda, ps_out, x, v,
+                                      last, hout);
+    });
 }
 
 __device__ __forceinline__ void cross3(const float *a, const float *b, float *o) {
@@ -864,10 +897,9 @@ __device__ __forceinline__ void cross3(const float *a, const float *b, float *o)
 
 // Pass A: vorticity omega and the XSPH sum (fluid neighbours only).
 template <class Sp>
-__device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+__device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps,
                                                const float4 *__restrict__ v, float4 *__restrict__ omega,
                                                float4 *__restrict__ vx) {
-    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     const float4 va4 = v[a];
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
@@ -956,19 +988,19 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, const Sp &sp
                         __fmaf_rn(ph.xsph_c, xs[2] * ws, va[2]), va4.w);
 }
 
+template <bool kTiles>
 __global__ void __launch_bounds__(256)
     k_vorticity_xsph(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ v,
                      float4 *__restrict__ omega, float4 *__restrict__ vx) {
-    vorticity_body(A, GlobalSpace<float4>{ps, v, A.type}, ps, v, omega, vx);
+    for_tiles<kTiles>(A, [&](uint32_t a) { vorticity_body(A, a, GlobalSpace<float4>{ps, v, A.type}, ps, v, omega, vx); });
 }
 
 // Pass B: eta = grad |omega|, N = eta / |eta|, f = eps (N x omega); v = vx + dt f.
 template <class Sp>
-__device__ __forceinline__ void apply_body(const GatherArgs &A, const Sp &sp, const float4 *__restrict__ ps,
+__device__ __forceinline__ void apply_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps,
                                            const float4 *__restrict__ omega, const float4 *__restrict__ vx,
                                            float4 *__restrict__ v, float4 *__restrict__ x,
                                            const HostParticlesOut *__restrict__ hout) {
-    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= A.n) return;
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         store_host_motion(hout, a, x[a], v[a]);
@@ -1028,11 +1060,14 @@ __device__ __forceinline__ void apply_body(const GatherArgs &A, const Sp &sp, co
     store_host_motion(hout, a, xn, vn);
 }
 
+template <bool kTiles>
 __global__ void __launch_bounds__(256)
     k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
                       const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
                       const HostParticlesOut *__restrict__ hout) {
-    apply_body(A, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
+    for_tiles<kTiles>(A, [&](uint32_t a) {
+        apply_body(A, a, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
+    });
 }
 
 // Colour diffusion of the ref profile (oclsph_kernel.h:281-303): each fluid particle
@@ -1192,6 +1227,8 @@ GatherArgs gather_args(const StepView &s) {
     A.over = s.over;
     A.near_stats = A.near ? s.near_stats : nullptr;
     A.plam = s.plam;
+    A.queue = nullptr;  // per launch, below
+    A.ppt = s.ppt ? s.ppt : 1;
     A.mass_range = s.mass_range;
     return A;
 }
@@ -1237,44 +1274,81 @@ void launch_reorder_cells(const StepView &s, cudaStream_t st) {
                                                       s.err, s.mass_range);
 }
 
+// Grid and tile counter of one gather launch (slot: its place among the step's
+// gather launches, each with its own counter).
+struct Launch {
+    unsigned grid;
+    GatherArgs A;
+};
+Launch gather_launch(const StepView &s, uint32_t slot) {
+    Launch L{grid_for(s.n, s.block), gather_args(s)};
+    if (s.queue) {
+        const uint64_t tiles = ((uint64_t)s.n + (uint64_t)s.block * L.A.ppt - 1) / ((uint64_t)s.block * L.A.ppt);
+        const uint64_t resident = (uint64_t)(s.sm_count > 0 ? s.sm_count : 152) * (2048u / (uint32_t)s.block);
+        L.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, resident));
+        L.A.queue = s.queue + slot;
+    }
+    return L;
+}
+
+// Gather launch slots of a step: the list build, then lambda and delta per iteration,
+// then the two vorticity passes.
+uint32_t slots_of_step(uint32_t iterations) { return 3 + 2 * iterations; }
+
+// Each gather kernel in two forms: a flat grid (one particle per thread) and a
+// persistent grid over the launch's tile queue; both compute the same bits.
+template <int P, int M>
+void run_lambda(const Launch &L, int block, cudaStream_t st, const float4 *ps, float *lambda, float *density) {
+    if (L.A.queue) k_lambda<P, M, true><<<L.grid, block, 0, st>>>(L.A, ps, lambda, density);
+    else k_lambda<P, M, false><<<L.grid, block, 0, st>>>(L.A, ps, lambda, density);
+}
+
+template <int P, int M>
+void run_delta(const Launch &L, int block, cudaStream_t st, const float4 *ps_in, const float *lambda, float4 *ps_out,
+               float4 *x, float4 *v, int last, const HostParticlesOut *hout) {
+    if (L.A.queue) k_delta<P, M, true><<<L.grid, block, 0, st>>>(L.A, ps_in, lambda, ps_out, x, v, last, hout);
+    else k_delta<P, M, false><<<L.grid, block, 0, st>>>(L.A, ps_in, lambda, ps_out, x, v, last, hout);
+}
+
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st) {
-    const GatherArgs A = gather_args(s);
-    const unsigned g = grid_for(s.n, s.block);
+    const Launch B = gather_launch(s, 0);
+    const Launch L = gather_launch(s, 1 + 2 * (uint32_t)iteration);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
-    if (iteration == 0 && A.cap) {
-        k_build_lists<<<g, s.block, 0, st>>>(A, ps);
-        if (ref) k_lambda<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+    if (iteration == 0 && L.A.cap) {
+        if (B.A.queue) k_build_lists<true><<<B.grid, s.block, 0, st>>>(B.A, ps);
+        else k_build_lists<false><<<B.grid, s.block, 0, st>>>(B.A, ps);
+        if (ref) run_lambda<FGB_PROFILE_REF, kFresh>(L, s.block, st, ps, s.lambda, s.density);
+        else run_lambda<FGB_PROFILE_BASELINE, kFresh>(L, s.block, st, ps, s.lambda, s.density);
     } else if (iteration == 0) {
-        if (ref) k_lambda<FGB_PROFILE_REF, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kBuild><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        if (ref) run_lambda<FGB_PROFILE_REF, kBuild>(L, s.block, st, ps, s.lambda, s.density);
+        else run_lambda<FGB_PROFILE_BASELINE, kBuild>(L, s.block, st, ps, s.lambda, s.density);
     } else {
-        if (ref) k_lambda<FGB_PROFILE_REF, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
-        else k_lambda<FGB_PROFILE_BASELINE, kCheck><<<g, s.block, 0, st>>>(A, ps, s.lambda, s.density);
+        if (ref) run_lambda<FGB_PROFILE_REF, kCheck>(L, s.block, st, ps, s.lambda, s.density);
+        else run_lambda<FGB_PROFILE_BASELINE, kCheck>(L, s.block, st, ps, s.lambda, s.density);
     }
 }
 
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,
                   cudaStream_t st) {
-    const GatherArgs A = gather_args(s);
-    const unsigned g = grid_for(s.n, s.block);
+    const Launch L = gather_launch(s, 2 + 2 * (uint32_t)iteration);
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
     const int l = last ? 1 : 0;
     if (iteration == 0) {
-        if (ref) k_delta<FGB_PROFILE_REF, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kFresh><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) run_delta<FGB_PROFILE_REF, kFresh>(L, s.block, st, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else run_delta<FGB_PROFILE_BASELINE, kFresh>(L, s.block, st, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     } else {
-        if (ref) k_delta<FGB_PROFILE_REF, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
-        else k_delta<FGB_PROFILE_BASELINE, kStored><<<g, s.block, 0, st>>>(A, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        if (ref) run_delta<FGB_PROFILE_REF, kStored>(L, s.block, st, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
+        else run_delta<FGB_PROFILE_BASELINE, kStored>(L, s.block, st, ps_in, s.lambda, ps_out, s.x1, s.v1, l, s.hout);
     }
 }
 
 void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st, const std::function<void()> &between) {
-    const GatherArgs A = gather_args(s);
-    const unsigned g = grid_for(s.n, s.block);
-    k_vorticity_xsph<<<g, s.block, 0, st>>>(A, ps, s.v1, s.omega, s.vx);
+    const Launch X = gather_launch(s, 1 + 2 * s.iterations), Y = gather_launch(s, 2 + 2 * s.iterations);
+    if (X.A.queue) k_vorticity_xsph<true><<<X.grid, s.block, 0, st>>>(X.A, ps, s.v1, s.omega, s.vx);
+    else k_vorticity_xsph<false><<<X.grid, s.block, 0, st>>>(X.A, ps, s.v1, s.omega, s.vx);
     if (between) between();
-    k_vorticity_apply<<<g, s.block, 0, st>>>(A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
+    if (Y.A.queue) k_vorticity_apply<true><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
+    else k_vorticity_apply<false><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

@@ -448,6 +448,8 @@ struct fgb_solver {
     struct Tuned {
         int block;
         float skin;
+        bool persistent;
+        uint32_t ppt;
     };
     std::map<uint32_t, Tuned> tuned;
     // row capacities (Verlet, hit) that batches grew to, per (profile, log2 n) bucket:
@@ -527,6 +529,12 @@ struct fgb_batch {
     uint32_t hit_cap = 64;
     uint32_t list_cap = 96;
     float skin_frac = 0.2f;
+    // persistent gathers: CTAs take tiles of ppt x block particles from per-launch
+    // counters (queue, zeroed at the start of every step) instead of a flat grid
+    bool persistent = false;
+    uint32_t ppt = 1;
+    Dev<uint32_t> queue;
+    int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
     int block = 128;  // threads per CTA of the gather kernels
@@ -623,6 +631,10 @@ struct fgb_batch {
         s.vx = vx.p;
         s.err = err.p;
         s.block = block;
+        s.queue = persistent ? queue.p : nullptr;
+        s.ppt = persistent ? ppt : 1;
+        s.iterations = iterations;
+        s.sm_count = sm_count;
         s.nlist = nlist.p;
         s.ncount = ncount.p;
         s.cap = nlist.p ? list_cap : 0;
@@ -679,6 +691,9 @@ struct fgb_batch {
         mark(k, st);
         if (io_up) FGB_CUDA(cudaStreamWaitEvent(st, io_up, cudaEventWaitExternal), "step: upload event");
         FGB_CUDA(cudaMemsetAsync(cells.p, 0, cells_n * sizeof(uint2), st), "step: clear cells");
+        if (persistent)
+            FGB_CUDA(cudaMemsetAsync(queue.p, 0, slots_of_step(iterations) * sizeof(uint32_t), st),
+                     "step: clear tile counters");
         FGB_CUDA(cudaMemsetAsync(mass_range.p, 0xff, 2 * sizeof(uint32_t), st), "step: clear mass range");
         if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
@@ -731,9 +746,11 @@ struct fgb_batch {
         FGB_CUDA(cudaEventCreate(&e0), "autotune event");
         FGB_CUDA(cudaEventCreate(&e1), "autotune event");
         uint32_t trials = 0, steps = 0;
-        auto trial = [&](int blk, float skin, float *ms) -> int {
+        auto trial = [&](int blk, float skin, bool pers, uint32_t per_thread, float *ms) -> int {
             block = blk;
             skin_frac = skin;
+            persistent = pers;
+            ppt = per_thread;
             for (auto &g : graph)
                 if (g) cudaGraphExecDestroy(g), g = nullptr;
             graphs_ok = false;
@@ -752,29 +769,42 @@ struct fgb_batch {
         int rc = FGB_OK;
         int best_block = block;
         float best_skin = skin_frac, best_ms = 3.4e38f, ms = 0.f;
+        bool best_pers = false;
+        uint32_t best_ppt = 1;
         const float skin0 = skin_frac;
+        // flat grids: CTA sizes, then skins; then persistent tile queues of 1 and 2
+        // particles per thread at the best of those
         for (int blk : {64, 128, 256}) {
-            rc = trial(blk, skin0, &ms);
+            rc = trial(blk, skin0, false, 1, &ms);
             if (rc) break;
             if (ms < best_ms) best_ms = ms, best_block = blk;
         }
         for (float skin : {0.1f, 0.15f, 0.25f, 0.3f}) {
             if (rc || skin == skin0) continue;
-            rc = trial(best_block, skin, &ms);
+            rc = trial(best_block, skin, false, 1, &ms);
             if (!rc && ms < best_ms) best_ms = ms, best_skin = skin;
+        }
+        for (uint32_t per_thread : {1u, 2u}) {
+            if (rc || !queue.p) continue;
+            rc = trial(best_block, best_skin, true, per_thread, &ms);
+            if (!rc && ms < best_ms) best_ms = ms, best_pers = true, best_ppt = per_thread;
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         block = best_block;
         skin_frac = best_skin;
+        persistent = best_pers;
+        ppt = best_ppt;
         for (auto &g : graph)
             if (g) cudaGraphExecDestroy(g), g = nullptr;
         graphs_ok = false;
         if (rc) return rc;
-        solver->tuned[tune_bucket(solver->params.profile, n)] = {best_block, best_skin};
+        solver->tuned[tune_bucket(solver->params.profile, n)] = {best_block, best_skin, best_pers, best_ppt};
         if (out) {
             out->block = (uint32_t)best_block;
             out->skin = best_skin;
+            out->persistent = best_pers ? 1u : 0u;
+            out->particles_per_thread = best_ppt;
             out->ms_per_step = best_ms;
             out->trials = trials;
             out->steps = steps;
@@ -1184,9 +1214,15 @@ static int batch_init(fgb_batch *b) {
         if (it != s->tuned.end()) {
             b->block = it->second.block;
             b->skin_frac = it->second.skin;
+            b->persistent = it->second.persistent;
+            b->ppt = it->second.ppt;
         }
     }
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
+    if (const char *e = getenv("FGB_PERSISTENT")) b->persistent = atoi(e) != 0;
+    if (const char *e = getenv("FGB_PPT")) b->ppt = (uint32_t)std::max(1, std::min(8, atoi(e)));
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+    FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
     if (b->list_cap) FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");

@@ -367,7 +367,10 @@ def test_autotune_changes_no_result():
     tuned_solver, plain_solver = SphSolver(params=params), SphSolver(params=params)
     a = Batch(tuned_solver, [(scenes.copy_particles(parts), cfg)])
     r = a.autotune(2)
-    assert r.block in (64, 128, 256) and r.trials == 7 and r.steps == 14
+    # three CTA sizes, the four other skins, then persistent tile queues of 1 and 2
+    # particles per thread
+    assert r.block in (64, 128, 256) and r.trials == 9 and r.steps == 18
+    assert r.persistent in (0, 1) and r.particles_per_thread in (1, 2)
     assert any(abs(r.skin - s) < 1e-6 for s in (0.1, 0.15, 0.2, 0.25, 0.3))
     b = Batch(plain_solver, [(scenes.copy_particles(parts), cfg)])
     b.step(r.steps)
@@ -380,6 +383,38 @@ def test_autotune_changes_no_result():
         x.close()
     tuned_solver.close()
     plain_solver.close()
+
+
+@pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
+def test_persistent_tile_queues_give_the_bits_of_flat_grids(profile, monkeypatch):
+    # the gathers as persistent grids whose CTAs take tiles of 1 or 3 x blockDim
+    # particles from a counter: each particle's work is unchanged, so three scenes of
+    # different sizes (tiles straddle scene boundaries), with obstacles, step to the
+    # same bits as with flat grids
+    params = capi.params(profile, H)
+    specs = []
+    for k, (dims, ext) in enumerate((((25, 16, 24), 2.5), ((10, 30, 10), 1.5), ((7, 7, 7), 0.7))):
+        parts, cfg = scenes.dam_break(dims, (ext, ext, ext), seed=130 + k)
+        parts["type"][::11] = capi.TYPE_OBSTACLE
+        specs.append((parts, cfg))
+    solver = SphSolver(params=params)
+    out = []
+    for env in ({"FGB_PERSISTENT": "0"}, {"FGB_PERSISTENT": "1", "FGB_PPT": "1"},
+                {"FGB_PERSISTENT": "1", "FGB_PPT": "3"}):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        b = Batch(solver, [(scenes.copy_particles(p), c) for p, c in specs])
+        b.step(10)
+        out.append([b.download(k) for k in range(len(specs))])
+        assert b.error_flags() == 0
+        b.close()
+        for k in env:
+            monkeypatch.delenv(k)
+    for run in out[1:]:
+        for k in range(len(specs)):
+            for f in ("id", "position", "velocity", "colour"):
+                assert (run[k][f] == out[0][k][f]).all(), (k, f)
+    solver.close()
 
 
 def test_advance_surface_frames_do_not_change_the_state():
