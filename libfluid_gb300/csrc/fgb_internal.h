@@ -60,6 +60,8 @@ struct StepView {
     float *lambda, *density;
     // the lambda pass's p* with lambda in w (the delta pass's neighbour reads; null: off)
     float4 *plam;
+    // the vorticity pass's p* with |omega| in w (the apply pass's neighbour reads; null: off)
+    float4 *pom;
     // {smallest mass, ~largest mass} as float bits, set by the grid build of each step
     uint32_t *mass_range;
     float4 *omega, *vx;

@@ -191,6 +191,7 @@ struct GatherArgs {
     // the lambda pass's p* with lambda in w, read by the delta pass (null: off), and the
     // batch's smallest and largest mass (float bits) of the step
     float4 *plam;
+    float4 *pom;  // the vorticity pass's p* with |omega| in w, read by the apply pass (null: off)
     const uint32_t *mass_range;
     // null: one particle per thread over a flat grid; else this launch's tile counter
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
@@ -254,6 +255,7 @@ struct GlobalSpace {
     // the delta pass's view of a candidate: its mass and its lambda
     __device__ __forceinline__ float mass(const float4 &pb) const { return pb.w; }
     __device__ __forceinline__ float lam(uint32_t b, const float4 &) const { return __ldg(&ex[b]); }
+    __device__ __forceinline__ T omega_of(uint32_t b) const { return __ldg(&ex[b]); }
     // Visit the particles of the 27 cells in walk order as f(b, p_b); loads run four
     // candidates ahead of the arithmetic.
     template <class F>
@@ -301,6 +303,15 @@ struct PackedSpace : GlobalSpace<float> {
     static constexpr bool kPacked = true;
     __device__ __forceinline__ float mass(const float4 &) const { return m; }
     __device__ __forceinline__ float lam(uint32_t, const float4 &pb) const { return pb.w; }
+};
+
+// The vorticity-apply pass's candidates through the vorticity pass's copy of p* with
+// each particle's |omega| in w (pom): one 16-byte load a neighbour instead of p* and
+// omega apart, when every particle of the batch has the same mass (`m`).
+struct PackedOmegaSpace : GlobalSpace<float4> {
+    float m;
+    static constexpr bool kPacked = true;
+    __device__ __forceinline__ float mass(const float4 &) const { return m; }
 };
 
 // Visit the c entries of particle a's row (particle-major, `cap` entries per row, cap
@@ -905,6 +916,10 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         omega[a] = make_float4(0.f, 0.f, 0.f, 0.f);
         vx[a] = va4;
+        if (A.pom) {
+            const float4 p = ps[a];
+            A.pom[a] = make_float4(p.x, p.y, p.z, 0.f);
+        }
         close_hits_empty(A, a);
         return;
     }
@@ -983,7 +998,9 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ws = ph.poly6f * ph.inv_rho0;
     const float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;
-    omega[a] = make_float4(ox, oy, oz, sqrtf(ox * ox + oy * oy + oz * oz));
+    const float om = sqrtf(ox * ox + oy * oy + oz * oz);
+    omega[a] = make_float4(ox, oy, oz, om);
+    if (A.pom) A.pom[a] = make_float4(pa.x, pa.y, pa.z, om);
     vx[a] = make_float4(__fmaf_rn(ph.xsph_c, xs[0] * ws, va[0]), __fmaf_rn(ph.xsph_c, xs[1] * ws, va[1]),
                         __fmaf_rn(ph.xsph_c, xs[2] * ws, va[2]), va4.w);
 }
@@ -1022,7 +1039,7 @@ __device__ __forceinline__ void apply_body(const GatherArgs &A, uint32_t a, cons
         const float r = sqrtf(r2);
         if (!(r >= kKernelEpsilon)) return;
         const float hr = ph.h - r;
-        const float sc = pb.w * ((hr * hr) / r) * (om_b().w - oa.w);
+        const float sc = sp.mass(pb) * ((hr * hr) / r) * (om_b().w - oa.w);
         e[0] = __fmaf_rn(sc, d[0], e[0]);
         e[1] = __fmaf_rn(sc, d[1], e[1]);
         e[2] = __fmaf_rn(sc, d[2], e[2]);
@@ -1030,11 +1047,18 @@ __device__ __forceinline__ void apply_body(const GatherArgs &A, uint32_t a, cons
     if (have_hits(A, a)) {
         // a near row (still marked) holds obstacles too; a filtered row fluid only
         const bool fluid_rows = !(A.near && A.near[a]);
-        auto row = [&](uint32_t b, const float4 &pb, auto om_b) { body(b, pb, om_b, fluid_rows); };
-        for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, row);
+        if constexpr (Sp::kPacked) {
+            auto row = [&](uint32_t b, const float4 &pb) {
+                body(b, pb, [&] { return make_float4(0.f, 0.f, 0.f, pb.w); }, fluid_rows);
+            };
+            for_row(A.hlist, A.hcap, a, A.hcount[a], sp, row);
+        } else {
+            auto row = [&](uint32_t b, const float4 &pb, auto om_b) { body(b, pb, om_b, fluid_rows); };
+            for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, row);
+        }
     } else {
         for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
-            body(b, pb, [&] { return sp.x(b); }, false);
+            body(b, pb, [&] { return Sp::kPacked ? make_float4(0.f, 0.f, 0.f, pb.w) : sp.omega_of(b); }, false);
         });
     }
     const float gs = ph.spikyf * ph.inv_rho0;
@@ -1065,8 +1089,14 @@ __global__ void __launch_bounds__(256)
     k_vorticity_apply(GatherArgs A, const float4 *__restrict__ ps, const float4 *__restrict__ omega,
                       const float4 *__restrict__ vx, float4 *__restrict__ v, float4 *__restrict__ x,
                       const HostParticlesOut *__restrict__ hout) {
+    // the vorticity pass's packed copy (p* with |omega| in w) when every mass is equal
+    const bool packed = A.pom && A.mass_range[0] == ~A.mass_range[1];
     for_tiles<kTiles>(A, [&](uint32_t a) {
-        apply_body(A, a, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
+        if (packed)
+            apply_body(A, a, PackedOmegaSpace{{A.pom, omega, A.type}, __uint_as_float(A.mass_range[0])}, ps, omega,
+                       vx, v, x, hout);
+        else
+            apply_body(A, a, GlobalSpace<float4>{ps, omega, A.type}, ps, omega, vx, v, x, hout);
     });
 }
 
@@ -1227,6 +1257,7 @@ GatherArgs gather_args(const StepView &s) {
     A.over = s.over;
     A.near_stats = A.near ? s.near_stats : nullptr;
     A.plam = s.plam;
+    A.pom = s.pom;
     A.queue = nullptr;  // per launch, below
     A.ppt = s.ppt ? s.ppt : 1;
     A.mass_range = s.mass_range;

@@ -540,6 +540,7 @@ struct fgb_batch {
     int block = 128;  // threads per CTA of the gather kernels
     Dev<float> lambda, density;
     Dev<float4> plam;             // the lambda pass's p* with lambda in w (delta reads)
+    Dev<float4> pom;              // the vorticity pass's p* with |omega| in w (apply reads)
     Dev<uint32_t> mass_range;     // {min mass, ~max mass} bits of the step
     Dev<float4> omega, vx;
     Dev<uint4> colour_sums;      // ref profile: per-cell channel sums (at the cell's first index)
@@ -625,6 +626,7 @@ struct fgb_batch {
         s.ps_b = ps[1].p;
         s.lambda = lambda.p;
         s.plam = plam.p;
+        s.pom = pom.p;
         s.mass_range = mass_range.p;
         s.density = density.p;
         s.omega = omega.p;
@@ -1105,6 +1107,7 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     FGB_CUDA(b->mass_range.alloc(2), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
+        if (!getenv("FGB_NO_PACKED_DELTA")) FGB_CUDA(b->pom.alloc(cap), "batch alloc");
         FGB_CUDA(b->omega.alloc(cap), "batch alloc");
         FGB_CUDA(b->vx.alloc(cap), "batch alloc");
     } else {
