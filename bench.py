@@ -370,7 +370,9 @@ def bench_large(params, steps=20, warmup=3, tune=True):
             "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3), "stages_ms_per_step": stages,
             "step_algorithmic_bytes": algo, "step_achieved_gbs": gbs, "hbm_peak_gbs": peak,
             "hbm_peak_kind": peak_kind, "step_hbm_frac": gbs / peak, "error_flags": flags, "surface": surface,
-            "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3)} if tuned else None)}
+            "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
+                           "persistent": bool(tuned.persistent),
+                           "particles_per_thread": int(tuned.particles_per_thread)} if tuned else None)}
 
 
 def bench_ref_profile(steps=30, warmup=5, tune=True):
@@ -772,6 +774,8 @@ def run_ours(args):
                        "sphere_collider": True, "l2": "flushed (256 MiB write) before every timed step",
                        "parallelism": f"replicas x{world}", "cuda_graph": True,
                        "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
+                                      "persistent": bool(tuned.persistent),
+                                      "particles_per_thread": int(tuned.particles_per_thread),
                                       "trial_steps": int(tuned.steps)} if tuned else None)},
             # direct: kernels read id/type/mass/colour/position/velocity (44 B) from the
             # caller's arrays and write them back; staged: pinned float4 x, float4 v,
