@@ -83,7 +83,6 @@ struct StepView {
     float4 *ps_grid;       // p* at grid build (displacements are measured from it)
     float *disp;           // |p - p_grid| per particle after the last delta pass
     uint32_t *cellmax;     // max displacement (float bits) per cell, same index as cells
-    float4 *boxes;         // per cell {lo, hi} of its particles' current positions (null: off)
     uint8_t *valid;        // per particle: 1 if its list is exact for the current positions
     // per-pass hit lists: the candidates of one pass that lie within h (and not on top
     // of the particle), in walk order; written by a lambda / vorticity pass, read by the
@@ -114,8 +113,6 @@ void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
-// the cell boxes of the positions ps (after the grid build and each delta pass)
-void launch_cell_boxes(const StepView &s, const float4 *ps, cudaStream_t st);
 // tile counters a step's gather launches use (persistent gathers)
 uint32_t slots_of_step(uint32_t iterations);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,

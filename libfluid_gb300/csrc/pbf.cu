@@ -197,10 +197,6 @@ struct GatherArgs {
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
     uint32_t ppt;
-    // cell boxes {lo, hi} per cell of the current positions (null: walks visit all 27
-    // cells); the walks' skip radii squared: the list build's, and every other pass's
-    const float4 *boxes;
-    float build_prune_r2, prune_r2;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -247,23 +243,6 @@ __device__ __forceinline__ bool use_list(const GatherArgs &A, const SceneDev &S,
 // pass's second array; fluid(b): whether b is not an obstacle.
 constexpr int kPrefetch = 4;
 
-// Cell boxes.  After the grid build and after every delta pass, k_cell_boxes writes
-// for each occupied cell the bounding box of its particles' current positions.  A
-// walk skips a cell whose box lies farther from the particle than every range test
-// of the pass: the squared distance to the box, formed from per-axis differences
-// that round no larger than those to any particle inside (rounding is monotonic), is
-// below any particle's squared distance up to the rounding of the squares and sums
-// (~1e-7 relative), so skipping only where it exceeds the pass's largest test radius
-// squared by 1e-5 drops no candidate that a test would have kept.  Walk order and sums
-// are unchanged.
-__device__ __forceinline__ bool box_beyond(const float4 *__restrict__ box, const float4 &pa, float prune) {
-    const float4 lo = __ldg(box), hi = __ldg(box + 1);
-    const float dx = pa.x < lo.x ? lo.x - pa.x : (pa.x > hi.x ? pa.x - hi.x : 0.f);
-    const float dy = pa.y < lo.y ? lo.y - pa.y : (pa.y > hi.y ? pa.y - hi.y : 0.f);
-    const float dz = pa.z < lo.z ? lo.z - pa.z : (pa.z > hi.z ? pa.z - hi.z : 0.f);
-    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) > prune;
-}
-
 template <class T>
 struct GlobalSpace {
     const float4 *ps;
@@ -278,11 +257,9 @@ struct GlobalSpace {
     __device__ __forceinline__ float lam(uint32_t b, const float4 &) const { return __ldg(&ex[b]); }
     __device__ __forceinline__ T omega_of(uint32_t b) const { return __ldg(&ex[b]); }
     // Visit the particles of the 27 cells in walk order as f(b, p_b); loads run four
-    // candidates ahead of the arithmetic.  With cell boxes, a cell whose particles all
-    // lie farther than sqrt(prune) from pa is skipped (see k_cell_boxes).
+    // candidates ahead of the arithmetic.
     template <class F>
-    __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f, const float4 &pa,
-                                         float prune) const {
+    __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f) const {
         const uint32_t m = morton_of(key, A.mbits);
         const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
         const int ex_ = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
@@ -296,10 +273,7 @@ struct GlobalSpace {
                 if (y < 0 || y > ey) continue;
                 const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
                 for (int x = x0; x <= x1; ++x) {
-                    const uint32_t cell = spread10((uint32_t)x) | yz;
-                    const uint2 c = __ldg(&tbl[cell]);
-                    if (c.x >= c.y) continue;
-                    if (A.boxes && box_beyond(A.boxes + 2 * ((size_t)S.table_base + cell), pa, prune)) continue;
+                    const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
                     visit(c.x, c.y, f);
                 }
             }
@@ -410,13 +384,11 @@ __device__ __forceinline__ void for_row_x(const uint32_t *__restrict__ base, uin
     }
 }
 
-// A's candidates: its Verlet row, or the walk of its 27 cells (cells farther than
-// sqrt(prune) skipped; every caller's range test is within prune)
 template <class Sp, class F>
 __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
-                                               bool list, const Sp &sp, F &&f, const float4 &pa, float prune) {
+                                               bool list, const Sp &sp, F &&f) {
     if (list) for_row(A.nlist, A.cap, a, A.ncount[a], sp, f);
-    else sp.walk(A, S, key, f, pa, prune);
+    else sp.walk(A, S, key, f);
 }
 
 // Hit lists.  A lambda pass and the delta pass after it read the same p*, so they
@@ -537,7 +509,7 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, cons
     for_candidates(A, S, a, key, false, sp, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
         if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
-    }, pa, A.build_prune_r2);
+    });
     A.ncount[a] = built.close();
     if (A.over) {  // one atomic per warp, when rows overflowed
         const unsigned m = __activemask();
@@ -638,7 +610,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
             }
         }
         if (A.hcap == 0 && MODE != kBuild) {
-            for_candidates(A, S, a, key, list, sp, body, pa, A.prune_r2);
+            for_candidates(A, S, a, key, list, sp, body);
         } else {
             // phase 1: range filter (and the Verlet list on the build pass)
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
@@ -652,7 +624,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
                 const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
                 if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
                 if (r2 <= (near_row ? A.near_r2 : hit_r2)) hits.add(b);
-            }, pa, A.prune_r2);
+            });
             if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
             if ((MODE == kBuild || MODE == kFresh) && A.over) {  // one atomic per warp, when rows overflowed
@@ -667,7 +639,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
             if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
             // phase 2: the kernel arithmetic over the hits, in walk order
             if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
-            else for_candidates(A, S, a, key, list, sp, body, pa, A.prune_r2);
+            else for_candidates(A, S, a, key, list, sp, body);
         }
     }
     float dens, lam;
@@ -852,7 +824,7 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, cons
     } else {
         for_candidates(A, S, a, key, use_list<MODE>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
             body(b, pb, [&] { return sp.lam(b, pb); });
-        }, pa, A.prune_r2);
+        });
     }
     float world[3];
     if (PROFILE == kRef) {
@@ -1005,7 +977,7 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
         auto any_row = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, false); };
         for_row_x(A.hlist, A.hcap, a, A.hcount[a], sp, any_row);
     } else if (A.hcap == 0) {
-        for_candidates(A, S, a, key, list, sp, any, pa, A.prune_r2);
+        for_candidates(A, S, a, key, list, sp, any);
     } else {
         // phase 1: fluid candidates within h; phase 2: the arithmetic over them
         HitWriter hits(A, a);
@@ -1014,13 +986,13 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
             const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
             if (r2 <= hit_r2 && (!S.obstacles || sp.fluid(b))) hits.add(b);
-        }, pa, A.prune_r2);
+        });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
             auto fluid = [&](uint32_t b, const float4 &pb, auto vel_b) { body(b, pb, vel_b, true); };
             for_row_x<true>(A.hlist, A.hcap, a, hits.count, sp, fluid);
         } else {
-            for_candidates(A, S, a, key, list, sp, any, pa, A.prune_r2);
+            for_candidates(A, S, a, key, list, sp, any);
         }
     }
     const float gs = ph.spikyf * ph.inv_rho0;
@@ -1087,7 +1059,7 @@ __device__ __forceinline__ void apply_body(const GatherArgs &A, uint32_t a, cons
     } else {
         for_candidates(A, S, a, key, use_list<kStored>(A, S, a, key), sp, [&](uint32_t b, const float4 &pb) {
             body(b, pb, [&] { return Sp::kPacked ? make_float4(0.f, 0.f, 0.f, pb.w) : sp.omega_of(b); }, false);
-        }, pa, A.prune_r2);
+        });
     }
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ex = e[0] * gs, ey = e[1] * gs, ez = e[2] * gs;
@@ -1207,29 +1179,6 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
     }
 }
 
-// The cell boxes of the walks (see box_beyond): at each occupied cell's first sorted
-// particle, the bounding box of the positions of the cell's particles, which are
-// contiguous in sorted order.
-__global__ void k_cell_boxes(const SceneDev *__restrict__ scenes, uint32_t n, uint32_t mbits,
-                             const uint32_t *__restrict__ keys, const uint2 *__restrict__ cells,
-                             const float4 *__restrict__ ps, float4 *__restrict__ boxes) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t key = keys[i];
-        if (i > 0 && keys[i - 1] == key) continue;
-        const SceneDev &S = scenes[scene_of(key, mbits)];
-        const size_t c = (size_t)S.table_base + morton_of(key, mbits);
-        const uint32_t end = min(cells[c].y, n);
-        float4 lo = ps[i], hi = lo;
-        for (uint32_t j = i + 1; j < end; ++j) {
-            const float4 p = ps[j];
-            lo.x = fminf(lo.x, p.x), lo.y = fminf(lo.y, p.y), lo.z = fminf(lo.z, p.z);
-            hi.x = fmaxf(hi.x, p.x), hi.y = fmaxf(hi.y, p.y), hi.z = fmaxf(hi.z, p.z);
-        }
-        boxes[2 * c] = lo;
-        boxes[2 * c + 1] = hi;
-    }
-}
-
 // Keys of the current positions (marching-cubes grid).
 __global__ void k_position_keys(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
                                 const uint32_t *__restrict__ keys_prev, const float4 *__restrict__ x,
@@ -1310,11 +1259,6 @@ GatherArgs gather_args(const StepView &s) {
     A.plam = s.plam;
     A.pom = s.pom;
     A.queue = nullptr;  // per launch, below
-    A.boxes = s.boxes;
-    A.build_prune_r2 = s.list_r2 * 1.00001f;
-    // every other pass tests within (h + near_skin)^2 (near rows), h^2 (1 + 1e-6) (hit
-    // filters) or h^2 (the arithmetic): the first is the largest
-    A.prune_r2 = std::max(s.near_r2, s.ph.hh * 1.00001f) * 1.00001f;
     A.ppt = s.ppt ? s.ppt : 1;
     A.mass_range = s.mass_range;
     return A;
@@ -1436,11 +1380,6 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
     if (between) between();
     if (Y.A.queue) k_vorticity_apply<true><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
     else k_vorticity_apply<false><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
-}
-
-void launch_cell_boxes(const StepView &s, const float4 *ps, cudaStream_t st) {
-    if (s.boxes)
-        k_cell_boxes<<<stream_grid(s.n), 256, 0, st>>>(s.scenes, s.n, s.mbits, s.keys_sorted, s.cells, ps, s.boxes);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

@@ -523,7 +523,6 @@ struct fgb_batch {
     Dev<uint16_t> ncount;
     Dev<float> disp;
     Dev<uint32_t> cellmax;
-    Dev<float4> boxes;  // per cell {lo, hi} of the current positions: the walks skip far cells
     Dev<uint8_t> valid;
     Dev<uint32_t> hlist;
     Dev<uint16_t> hcount;
@@ -648,7 +647,6 @@ struct fgb_batch {
         s.ps_grid = ps_grid.p;
         s.disp = disp.p;
         s.cellmax = cellmax.p;
-        s.boxes = boxes.p;
         s.valid = valid.p;
         s.hlist = hlist.p;
         s.hcount = hcount.p;
@@ -702,10 +700,6 @@ struct fgb_batch {
         if (cellmax.p) FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
         launch_reorder_cells(s, st);
         l += 1;
-        if (s.boxes) {
-            launch_cell_boxes(s, ps_grid.p, st);
-            l += 1;
-        }
         if (ph.profile == FGB_PROFILE_REF) {
             launch_diffuse(s, colour_sums.p, colour_count.p, st);
             l += 2;
@@ -725,12 +719,6 @@ struct fgb_batch {
             if (it > 0 && cellmax.p)
                 FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
-            // the boxes of the new positions, for the walks of the passes after it (the
-            // ref profile's last delta pass has none)
-            if (s.boxes && (it + 1 < iterations || ph.profile != FGB_PROFILE_REF)) {
-                launch_cell_boxes(s, pout, st);
-                l += 1;
-            }
             mark(k, st);
             l += (it == 0 && s.cap) ? 3 : 2;
             pin = pout;
@@ -1215,7 +1203,6 @@ static int batch_init(fgb_batch *b) {
     }
     FGB_CUDA(b->ids_dev.alloc(n), "batch alloc");
     FGB_CUDA(b->cells.alloc(std::max<uint64_t>(table, 1)), "batch alloc cells");
-    if (!getenv("FGB_NO_BOXES")) FGB_CUDA(b->boxes.alloc(2 * std::max<uint64_t>(table, 1)), "batch alloc cell boxes");
     {
         auto it = s->caps.find(tune_bucket(p.profile, n));
         if (it != s->caps.end()) {
@@ -1473,8 +1460,8 @@ static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64
     scene_geometry(p, c, S);
     const uint64_t table = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
     uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * list_words + 2 + 2 + 4 + 1;
-    per_particle += p.profile != FGB_PROFILE_REF ? 32 + 32 : 20 + 16;  // + the packed neighbour copies
-    uint64_t bytes = per_particle * n + (12 + 32) * table;             // cells, maxima, boxes
+    per_particle += p.profile != FGB_PROFILE_REF ? 32 : 20;
+    uint64_t bytes = per_particle * n + 12 * table;
     if (mesh && S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1) {
         const uint64_t samples = (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];
         const uint64_t cubes = (uint64_t)(S.lat[0] - 1) * (S.lat[1] - 1) * (S.lat[2] - 1);
