@@ -1460,7 +1460,7 @@ static uint64_t scene_footprint(const fgb_params &p, const fgb_config &c, uint64
     scene_geometry(p, c, S);
     const uint64_t table = (uint64_t)morton3(S.ext[0], S.ext[1], S.ext[2]) + 1;
     uint64_t per_particle = 64 + 24 + 16 + 8 + 1 + 48 + 8 + 4ull * list_words + 2 + 2 + 4 + 1;
-    per_particle += p.profile != FGB_PROFILE_REF ? 32 : 20;
+    per_particle += p.profile != FGB_PROFILE_REF ? 32 + 32 : 20 + 16;  // + the packed neighbour copies
     uint64_t bytes = per_particle * n + 12 * table;
     if (mesh && S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1) {
         const uint64_t samples = (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];
