@@ -71,6 +71,8 @@ struct StepView {
     // of the step (slots_of_step), ppt particles per thread of a tile
     uint32_t *queue;
     uint32_t ppt;
+    // {1 while steps build Verlet lists, movers of the step} (null: lists every step)
+    uint32_t *list_policy;
     uint32_t iterations;
     int sm_count;
     // per-step neighbour lists (Verlet lists with a skin), particle-major rows of cap
@@ -113,6 +115,8 @@ void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i
 void launch_predict_keys(const StepView &s, cudaStream_t st);
 void launch_reorder_cells(const StepView &s, cudaStream_t st);
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st);
+// at the end of a step: whether the next one builds Verlet lists
+void launch_list_policy(const StepView &s, cudaStream_t st);
 // tile counters a step's gather launches use (persistent gathers)
 uint32_t slots_of_step(uint32_t iterations);
 void launch_delta(const StepView &s, const float4 *ps_in, float4 *ps_out, int iteration, bool last,

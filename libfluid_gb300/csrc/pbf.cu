@@ -197,6 +197,9 @@ struct GatherArgs {
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
     uint32_t ppt;
+    // null, or [0] 1 while this step builds Verlet lists and near rows, [1] particles
+    // of the step's last delta pass that moved more than half the skin (k_list_policy)
+    uint32_t *list_policy;
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -496,6 +499,10 @@ __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
 template <class Sp>
 __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps) {
     if (a >= A.n) return;
+    if (A.list_policy && !A.list_policy[0]) {  // lists off this step: every pass walks
+        A.ncount[a] = kListOverflow;
+        return;
+    }
     if (A.type[a] == FGB_TYPE_OBSTACLE) {
         A.ncount[a] = 0;
         return;
@@ -615,7 +622,8 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
             // phase 1: range filter (and the Verlet list on the build pass)
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
-            const bool near_row = (MODE == kBuild || MODE == kFresh) && A.near;
+            const bool near_row =
+                (MODE == kBuild || MODE == kFresh) && A.near && !(A.list_policy && !A.list_policy[0]);
             // membership only (the arithmetic re-tests every entry exactly): a contracted
             // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
             const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
@@ -636,7 +644,8 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
                     if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
                 }
             }
-            if (near_row) A.near[a] = A.hcap && hits.count <= A.hcap ? 1 : 0;
+            // the first pass sets every mark (none when this step builds no near rows)
+            if ((MODE == kBuild || MODE == kFresh) && A.near) A.near[a] = near_row && A.hcap && hits.count <= A.hcap ? 1 : 0;
             // phase 2: the kernel arithmetic over the hits, in walk order
             if (A.hcap && hits.count <= A.hcap) for_row<true>(A.hlist, A.hcap, a, hits.count, sp, body);
             else for_candidates(A, S, a, key, list, sp, body);
@@ -860,6 +869,11 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, cons
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);
         A.disp[a] = d;
         atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
+        if (last && A.list_policy) {  // one atomic per warp, for k_list_policy
+            const unsigned m = __activemask();
+            const unsigned far = __ballot_sync(m, d > 0.5f * A.skin);
+            if (far && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.list_policy[1], (uint32_t)__popc(far));
+        }
     }
     if (last) {
         const float4 xa = x[a];
@@ -1179,6 +1193,17 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
     }
 }
 
+// At the end of a step: whether the next step builds Verlet lists and near rows.  A
+// list holds while its particle and every candidate together moved less than the
+// skin; when more than 1% of the particles moved over half the skin in a step, nearly
+// every 27-cell neighbourhood holds one (a violent flow: lists would be built and then
+// fail their bound at every later pass), so the next step walks instead.  Sums are
+// the same either way.
+__global__ void k_list_policy(uint32_t *policy, uint32_t n) {
+    policy[0] = (uint64_t)policy[1] * 100u <= (uint64_t)n ? 1u : 0u;
+    policy[1] = 0u;
+}
+
 // Keys of the current positions (marching-cubes grid).
 __global__ void k_position_keys(const SceneDev *__restrict__ scenes, Phys ph, uint32_t n, uint32_t mbits,
                                 const uint32_t *__restrict__ keys_prev, const float4 *__restrict__ x,
@@ -1259,6 +1284,7 @@ GatherArgs gather_args(const StepView &s) {
     A.plam = s.plam;
     A.pom = s.pom;
     A.queue = nullptr;  // per launch, below
+    A.list_policy = s.cap ? s.list_policy : nullptr;
     A.ppt = s.ppt ? s.ppt : 1;
     A.mass_range = s.mass_range;
     return A;
@@ -1380,6 +1406,10 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
     if (between) between();
     if (Y.A.queue) k_vorticity_apply<true><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
     else k_vorticity_apply<false><<<Y.grid, s.block, 0, st>>>(Y.A, ps, s.omega, s.vx, s.v1, s.x1, s.hout);
+}
+
+void launch_list_policy(const StepView &s, cudaStream_t st) {
+    if (s.list_policy && s.cap) k_list_policy<<<1, 1, 0, st>>>(s.list_policy, s.n);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

@@ -534,6 +534,7 @@ struct fgb_batch {
     bool persistent = false;
     uint32_t ppt = 1;
     Dev<uint32_t> queue;
+    Dev<uint32_t> list_policy;  // {lists this step, movers}: k_list_policy
     int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
@@ -634,6 +635,7 @@ struct fgb_batch {
         s.err = err.p;
         s.block = block;
         s.queue = persistent ? queue.p : nullptr;
+        s.list_policy = list_policy.p;
         s.ppt = persistent ? ppt : 1;
         s.iterations = iterations;
         s.sm_count = sm_count;
@@ -727,6 +729,10 @@ struct fgb_batch {
             launch_velocity_terms(s, pin, st, [&] { mark(k, st); });
             mark(k, st);
             l += 2;
+        }
+        if (s.list_policy && s.cap) {
+            launch_list_policy(s, st);
+            l += 1;
         }
         if (over.p)
             FGB_CUDA(cudaMemcpyAsync(st_over.p, over.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
@@ -1226,6 +1232,11 @@ static int batch_init(fgb_batch *b) {
     if (const char *e = getenv("FGB_PPT")) b->ppt = (uint32_t)std::max(1, std::min(8, atoi(e)));
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, s->device);
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
+    if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
+        FGB_CUDA(b->list_policy.alloc(2), "batch alloc");
+        const uint32_t init[2] = {1u, 0u};  // the first step builds lists
+        FGB_CUDA(cudaMemcpy(b->list_policy.p, init, sizeof(init), cudaMemcpyHostToDevice), "batch alloc");
+    }
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
     if (b->list_cap) FGB_CUDA(b->cellmax.alloc(std::max<uint64_t>(table, 1)), "batch alloc");
