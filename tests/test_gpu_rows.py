@@ -31,7 +31,10 @@ def _overflow(b):
 
 
 def _run(params, parts, cfg, caps, steps):
+    # lists every step (the list policy would stop building them in violent steps,
+    # which leaves no rows to grow)
     env = {"FGB_LIST_CAP": str(caps[0]), "FGB_HIT_CAP": str(caps[1])} if caps else {}
+    env["FGB_LIST_POLICY"] = "0"
     os.environ.update(env)
     try:
         solver = SphSolver(params=params)
@@ -59,3 +62,31 @@ def test_rows_grow_from_small_capacities_without_changing_results(profile):
     assert over[-1] < 0.02           # and the rows have grown past the neighbour counts
     roomy, _ = _run(params, parts, cfg, (512, 512), 12)
     _same(grown, roomy)
+
+
+@pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
+def test_list_policy_changes_no_result(profile):
+    # the list policy stops building Verlet lists and near rows for a step after one
+    # in which more than 1% of the particles moved over half the skin: every pass then
+    # walks its cells.  A violent scene (a dam break onto a sphere) reaches such steps;
+    # the state after them equals that with lists built every step, bit for bit.
+    params = capi.params(profile, H)
+    parts, cfg = scenes.dam_break((20, 16, 20), (2.0, 1.6, 2.0), seed=93, sphere=(1.0, 0.3, 1.0, 0.3))
+    out = {}
+    for policy in ("1", "0"):
+        os.environ["FGB_LIST_POLICY"] = policy
+        try:
+            solver = SphSolver(params=params)
+            b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+        finally:
+            del os.environ["FGB_LIST_POLICY"]
+        off = 0
+        for _ in range(40):
+            b.step(1)
+            off += _overflow(b) == 1.0  # every row marked: no lists this step
+        out[policy] = (b.download(0), off)
+        assert b.error_flags() == 0
+        b.close()
+        solver.close()
+    assert out["1"][1] > 0 and out["0"][1] == 0
+    _same(out["1"][0], out["0"][0])
