@@ -867,8 +867,11 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, cons
         const float4 g = A.ps_grid[a];
         const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);
-        A.disp[a] = d;
-        atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
+        // (a step without lists or near rows checks no bound)
+        if (!(A.list_policy && !A.list_policy[0])) {
+            A.disp[a] = d;
+            atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
+        }
         if (last && A.list_policy) {  // one atomic per warp, for k_list_policy
             const unsigned m = __activemask();
             const unsigned far = __ballot_sync(m, d > 0.5f * A.skin);
