@@ -197,8 +197,9 @@ struct GatherArgs {
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
     uint32_t ppt;
-    // null, or [0] 1 while this step builds Verlet lists and near rows, [1] particles
-    // of the step's last delta pass that moved more than half the skin (k_list_policy)
+    // null, or per scene s: [3s] 1 while this step builds the scene's Verlet lists and
+    // near rows, [3s + 1] its fluid particles that the step's last delta pass moved
+    // more than half the skin and [3s + 2] all its fluid particles (k_list_policy)
     uint32_t *list_policy;
 };
 
@@ -492,6 +493,11 @@ __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
     }
 }
 
+// Whether this step builds scene sc's Verlet lists and near rows (k_list_policy).
+__device__ __forceinline__ bool lists_on(const GatherArgs &A, uint32_t sc) {
+    return !A.list_policy || A.list_policy[3 * sc] != 0u;
+}
+
 // The step's Verlet lists on their own: each particle walks its 27 cells and keeps, in
 // walk order, every candidate within h + skin.  The first lambda pass then filters the
 // fresh lists (near rows) instead of walking, so the walk carries one row writer and
@@ -499,7 +505,7 @@ __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
 template <class Sp>
 __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps) {
     if (a >= A.n) return;
-    if (A.list_policy && !A.list_policy[0]) {  // lists off this step: every pass walks
+    if (!lists_on(A, scene_of(A.keys[a], A.mbits))) {  // no lists this step: every pass walks
         A.ncount[a] = kListOverflow;
         return;
     }
@@ -623,7 +629,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
             RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
             const bool near_row =
-                (MODE == kBuild || MODE == kFresh) && A.near && !(A.list_policy && !A.list_policy[0]);
+                (MODE == kBuild || MODE == kFresh) && A.near && lists_on(A, scene_of(key, A.mbits));
             // membership only (the arithmetic re-tests every entry exactly): a contracted
             // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
             const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
@@ -868,14 +874,19 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, cons
         const float ex = q[0] - g.x, ey = q[1] - g.y, ez = q[2] - g.z;
         const float d = sqrtf(ex * ex + ey * ey + ez * ez);
         // (a step without lists or near rows checks no bound)
-        if (!(A.list_policy && !A.list_policy[0])) {
+        const uint32_t sc = scene_of(key, A.mbits);
+        if (lists_on(A, sc)) {
             A.disp[a] = d;
             atomicMax(&A.cellmax[S.table_base + morton_of(key, A.mbits)], __float_as_uint(d));
         }
-        if (last && A.list_policy) {  // one atomic per warp, for k_list_policy
+        if (last && A.list_policy) {  // one atomic pair per scene of the warp, for k_list_policy
             const unsigned m = __activemask();
-            const unsigned far = __ballot_sync(m, d > 0.5f * A.skin);
-            if (far && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.list_policy[1], (uint32_t)__popc(far));
+            const unsigned grp = __match_any_sync(m, sc);
+            const unsigned far = __ballot_sync(m, d > 0.5f * A.skin) & grp;
+            if ((threadIdx.x & 31u) == (unsigned)(__ffs(grp) - 1)) {
+                if (far) atomicAdd(&A.list_policy[3 * sc + 1], (uint32_t)__popc(far));
+                atomicAdd(&A.list_policy[3 * sc + 2], (uint32_t)__popc(grp));
+            }
         }
     }
     if (last) {
@@ -1196,15 +1207,18 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
     }
 }
 
-// At the end of a step: whether the next step builds Verlet lists and near rows.  A
-// list holds while its particle and every candidate together moved less than the
-// skin; when more than 1% of the particles moved over half the skin in a step, nearly
-// every 27-cell neighbourhood holds one (a violent flow: lists would be built and then
-// fail their bound at every later pass), so the next step walks instead.  Sums are
-// the same either way.
-__global__ void k_list_policy(uint32_t *policy, uint32_t n) {
-    policy[0] = (uint64_t)policy[1] * 100u <= (uint64_t)n ? 1u : 0u;
-    policy[1] = 0u;
+// At the end of a step, per scene: whether the next step builds its Verlet lists and
+// near rows.  A list holds while its particle and every candidate together moved less
+// than the skin; when more than 1% of a scene's fluid particles moved over half the
+// skin in a step, nearly every 27-cell neighbourhood of the scene holds one (a violent
+// flow: lists would be built and then fail their bound at every later pass), so the
+// scene's next step walks instead.  Sums are the same either way.
+__global__ void k_list_policy(uint32_t *policy, uint32_t n_scenes) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_scenes; s += gridDim.x * blockDim.x) {
+        uint32_t *p = policy + 3 * s;
+        p[0] = (uint64_t)p[1] * 100u <= (uint64_t)p[2] ? 1u : 0u;
+        p[1] = p[2] = 0u;
+    }
 }
 
 // Keys of the current positions (marching-cubes grid).
@@ -1412,7 +1426,7 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
 }
 
 void launch_list_policy(const StepView &s, cudaStream_t st) {
-    if (s.list_policy && s.cap) k_list_policy<<<1, 1, 0, st>>>(s.list_policy, s.n);
+    if (s.list_policy && s.cap) k_list_policy<<<(s.n_scenes + 255) / 256, 256, 0, st>>>(s.list_policy, s.n_scenes);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

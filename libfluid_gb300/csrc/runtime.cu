@@ -604,6 +604,7 @@ struct fgb_batch {
         s.wells = d_wells.p;
         s.tris = d_tris.p;
         s.n = (uint32_t)n;
+        s.n_scenes = n_scenes;
         s.mbits = mbits;
         s.ph = ph;
         s.x0 = x[c].p;
@@ -1233,9 +1234,11 @@ static int batch_init(fgb_batch *b) {
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, s->device);
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
-        FGB_CUDA(b->list_policy.alloc(2), "batch alloc");
-        const uint32_t init[2] = {1u, 0u};  // the first step builds lists
-        FGB_CUDA(cudaMemcpy(b->list_policy.p, init, sizeof(init), cudaMemcpyHostToDevice), "batch alloc");
+        FGB_CUDA(b->list_policy.alloc(3 * (uint64_t)b->n_scenes), "batch alloc");
+        std::vector<uint32_t> init(3 * (size_t)b->n_scenes, 0u);
+        for (uint32_t k = 0; k < b->n_scenes; ++k) init[3 * k] = 1u;  // the first step builds lists
+        FGB_CUDA(cudaMemcpy(b->list_policy.p, init.data(), init.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                 "batch alloc");
     }
     if (b->list_cap > 4096) b->list_cap = 4096;
     b->list_cap = (b->list_cap + 3u) & ~3u;  // rows move as 16-byte vectors
