@@ -197,10 +197,9 @@ struct GatherArgs {
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
     uint32_t ppt;
-    // null, or per scene s: [3s] 1 while this step builds the scene's Verlet lists and
-    // near rows, [3s + 1] its fluid particles that the step's last delta pass moved
-    // more than half the skin and [3s + 2] all its fluid particles (k_list_policy)
+    // null, or per scene: kPolicyWords words of k_list_policy's state
     uint32_t *list_policy;
+    int count_lists;  // this lambda pass samples how many particles could use their list
 };
 
 enum ListMode { kBuild = 0, kFresh = 1, kCheck = 2, kStored = 3 };
@@ -450,6 +449,26 @@ __device__ __forceinline__ void close_hits_empty(const GatherArgs &A, uint32_t a
     if (A.hcap) A.hcount[a] = 0;
 }
 
+// k_list_policy's words per scene: [0] 1 while steps build the scene's Verlet lists and
+// near rows; counts of the current step: [1] fluid particles that its last delta pass
+// moved more than half the skin, [2] all fluid particles of that pass, [3] particles of
+// its second lambda pass that ran on a near row or a list that held, [4] those that
+// walked; [5] steps since the lists were turned off.
+constexpr uint32_t kPolicyWords = 6;
+
+// The list policy's sample: per scene of the warp, the particles whose list (or near
+// row) served this pass and those that walked.
+__device__ __forceinline__ void count_list_use(const GatherArgs &A, uint32_t key, bool used) {
+    const uint32_t sc = scene_of(key, A.mbits);
+    const unsigned m = __activemask();
+    const unsigned grp = __match_any_sync(m, sc);
+    const unsigned on = __ballot_sync(m, used) & grp;
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(grp) - 1)) {
+        if (on) atomicAdd(&A.list_policy[kPolicyWords * sc + 3], (uint32_t)__popc(on));
+        if (grp & ~on) atomicAdd(&A.list_policy[kPolicyWords * sc + 4], (uint32_t)__popc(grp & ~on));
+    }
+}
+
 // One count per warp of a checked pass: whether it ran on its near rows.
 __device__ __forceinline__ void count_near(const GatherArgs &A, bool on_rows) {
     if (!A.near_stats) return;
@@ -495,7 +514,7 @@ __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
 
 // Whether this step builds scene sc's Verlet lists and near rows (k_list_policy).
 __device__ __forceinline__ bool lists_on(const GatherArgs &A, uint32_t sc) {
-    return !A.list_policy || A.list_policy[3 * sc] != 0u;
+    return !A.list_policy || A.list_policy[kPolicyWords * sc] != 0u;
 }
 
 // The step's Verlet lists on their own: each particle walks its 27 cells and keeps, in
@@ -603,6 +622,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
         }
         done = __all_sync(__activemask(), ok);
         count_near(A, done);
+        if (done && A.count_lists && A.list_policy) count_list_use(A, key, true);
         if (done) for_hits(A, a, sp, body);
         else A.near[a] = 0;
     }
@@ -614,6 +634,7 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
         // candidates within h + skin in walk order); the baseline profile is faster with
         // the choice per lane.
         if constexpr (MODE == kCheck && PROFILE == kRef) list = __all_sync(__activemask(), list);
+        if (MODE == kCheck && A.count_lists && A.list_policy) count_list_use(A, key, list);
         if (MODE == kCheck && A.near_stats) {
             const unsigned m = __activemask();
             const unsigned on = __ballot_sync(m, list);
@@ -884,8 +905,8 @@ __device__ __forceinline__ void delta_body(const GatherArgs &A, uint32_t a, cons
             const unsigned grp = __match_any_sync(m, sc);
             const unsigned far = __ballot_sync(m, d > 0.5f * A.skin) & grp;
             if ((threadIdx.x & 31u) == (unsigned)(__ffs(grp) - 1)) {
-                if (far) atomicAdd(&A.list_policy[3 * sc + 1], (uint32_t)__popc(far));
-                atomicAdd(&A.list_policy[3 * sc + 2], (uint32_t)__popc(grp));
+                if (far) atomicAdd(&A.list_policy[kPolicyWords * sc + 1], (uint32_t)__popc(far));
+                atomicAdd(&A.list_policy[kPolicyWords * sc + 2], (uint32_t)__popc(grp));
             }
         }
     }
@@ -1209,15 +1230,27 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
 
 // At the end of a step, per scene: whether the next step builds its Verlet lists and
 // near rows.  A list holds while its particle and every candidate together moved less
-// than the skin; when more than 1% of a scene's fluid particles moved over half the
-// skin in a step, nearly every 27-cell neighbourhood of the scene holds one (a violent
-// flow: lists would be built and then fail their bound at every later pass), so the
-// scene's next step walks instead.  Sums are the same either way.
+// than the skin.  In a violent flow some particle of nearly every 27-cell
+// neighbourhood moves that far within a step, the lists fail their bound at every later
+// pass and building them is wasted: the scene's next steps walk instead, until it
+// calms.  Sums are the same either way.
 __global__ void k_list_policy(uint32_t *policy, uint32_t n_scenes) {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_scenes; s += gridDim.x * blockDim.x) {
-        uint32_t *p = policy + 3 * s;
-        p[0] = (uint64_t)p[1] * 100u <= (uint64_t)p[2] ? 1u : 0u;
-        p[1] = p[2] = 0u;
+        uint32_t *p = policy + kPolicyWords * s;
+        if (p[0]) {
+            // lists were built: keep them while at least a quarter of the second pass's
+            // particles could use them (the list build and its filter cost about what a
+            // quarter of the later walks saves)
+            const uint64_t seen = (uint64_t)p[3] + p[4];
+            p[0] = seen == 0 || 4ull * p[3] >= seen ? 1u : 0u;
+            p[5] = 0u;
+        } else {
+            // walking: build again once the scene has calmed (at most 1% of its particles
+            // moved over half the skin), and try every 8th step anyway
+            p[5] += 1u;
+            p[0] = (uint64_t)p[1] * 100u <= (uint64_t)p[2] || p[5] >= 8u ? 1u : 0u;
+        }
+        p[1] = p[2] = p[3] = p[4] = 0u;
     }
 }
 
@@ -1302,6 +1335,7 @@ GatherArgs gather_args(const StepView &s) {
     A.pom = s.pom;
     A.queue = nullptr;  // per launch, below
     A.list_policy = s.cap ? s.list_policy : nullptr;
+    A.count_lists = 0;  // the second lambda pass's launch sets it
     A.ppt = s.ppt ? s.ppt : 1;
     A.mass_range = s.mass_range;
     return A;
@@ -1386,7 +1420,8 @@ void run_delta(const Launch &L, int block, cudaStream_t st, const float4 *ps_in,
 
 void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStream_t st) {
     const Launch B = gather_launch(s, 0);
-    const Launch L = gather_launch(s, 1 + 2 * (uint32_t)iteration);
+    Launch L = gather_launch(s, 1 + 2 * (uint32_t)iteration);
+    L.A.count_lists = iteration == 1;
     const bool ref = s.ph.profile == FGB_PROFILE_REF;
     if (iteration == 0 && L.A.cap) {
         if (B.A.queue) k_build_lists<true><<<B.grid, s.block, 0, st>>>(B.A, ps);

@@ -1234,9 +1234,9 @@ static int batch_init(fgb_batch *b) {
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, s->device);
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
-        FGB_CUDA(b->list_policy.alloc(3 * (uint64_t)b->n_scenes), "batch alloc");
-        std::vector<uint32_t> init(3 * (size_t)b->n_scenes, 0u);
-        for (uint32_t k = 0; k < b->n_scenes; ++k) init[3 * k] = 1u;  // the first step builds lists
+        FGB_CUDA(b->list_policy.alloc(6 * (uint64_t)b->n_scenes), "batch alloc");
+        std::vector<uint32_t> init(6 * (size_t)b->n_scenes, 0u);
+        for (uint32_t k = 0; k < b->n_scenes; ++k) init[6 * k] = 1u;  // the first step builds lists
         FGB_CUDA(cudaMemcpy(b->list_policy.p, init.data(), init.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
                  "batch alloc");
     }
