@@ -73,6 +73,7 @@ struct StepView {
     uint32_t ppt;
     // {1 while steps build Verlet lists, movers of the step} (null: lists every step)
     uint32_t *list_policy;
+    uint32_t list_min_use;  // percent of a pass's particles that keeps lists on
     uint32_t n_scenes;
     uint32_t iterations;
     int sm_count;

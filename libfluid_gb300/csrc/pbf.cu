@@ -1234,15 +1234,15 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
 // neighbourhood moves that far within a step, the lists fail their bound at every later
 // pass and building them is wasted: the scene's next steps walk instead, until it
 // calms.  Sums are the same either way.
-__global__ void k_list_policy(uint32_t *policy, uint32_t n_scenes) {
+__global__ void k_list_policy(uint32_t *policy, uint32_t n_scenes, uint32_t min_use_pct) {
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_scenes; s += gridDim.x * blockDim.x) {
         uint32_t *p = policy + kPolicyWords * s;
         if (p[0]) {
-            // lists were built: keep them while at least a quarter of the second pass's
-            // particles could use them (the list build and its filter cost about what a
-            // quarter of the later walks saves)
+            // lists were built: keep them while at least min_use_pct (25) percent of the
+            // second pass's particles could use them (the list build and its filter cost
+            // about what a quarter of the later walks saves)
             const uint64_t seen = (uint64_t)p[3] + p[4];
-            p[0] = seen == 0 || 4ull * p[3] >= seen ? 1u : 0u;
+            p[0] = seen == 0 || 100ull * p[3] >= (uint64_t)min_use_pct * seen ? 1u : 0u;
             p[5] = 0u;
         } else {
             // walking: build again once the scene has calmed (at most 1% of its particles
@@ -1461,7 +1461,8 @@ void launch_velocity_terms(const StepView &s, const float4 *ps, cudaStream_t st,
 }
 
 void launch_list_policy(const StepView &s, cudaStream_t st) {
-    if (s.list_policy && s.cap) k_list_policy<<<(s.n_scenes + 255) / 256, 256, 0, st>>>(s.list_policy, s.n_scenes);
+    if (s.list_policy && s.cap)
+        k_list_policy<<<(s.n_scenes + 255) / 256, 256, 0, st>>>(s.list_policy, s.n_scenes, s.list_min_use);
 }
 
 void launch_diffuse(const StepView &s, uint4 *agg, uint32_t *count, cudaStream_t st) {

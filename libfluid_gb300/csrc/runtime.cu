@@ -534,7 +534,8 @@ struct fgb_batch {
     bool persistent = false;
     uint32_t ppt = 1;
     Dev<uint32_t> queue;
-    Dev<uint32_t> list_policy;  // {lists this step, movers}: k_list_policy
+    Dev<uint32_t> list_policy;  // per scene: k_list_policy's state
+    uint32_t list_min_use = 25;  // FGB_LIST_MIN_USE: percent of particles using lists that keeps them
     int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
@@ -637,6 +638,7 @@ struct fgb_batch {
         s.block = block;
         s.queue = persistent ? queue.p : nullptr;
         s.list_policy = list_policy.p;
+        s.list_min_use = list_min_use;
         s.ppt = persistent ? ppt : 1;
         s.iterations = iterations;
         s.sm_count = sm_count;
@@ -1235,6 +1237,7 @@ static int batch_init(fgb_batch *b) {
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
         FGB_CUDA(b->list_policy.alloc(6 * (uint64_t)b->n_scenes), "batch alloc");
+        if (const char *e = getenv("FGB_LIST_MIN_USE")) b->list_min_use = (uint32_t)std::max(0, std::min(101, atoi(e)));
         std::vector<uint32_t> init(6 * (size_t)b->n_scenes, 0u);
         for (uint32_t k = 0; k < b->n_scenes; ++k) init[6 * k] = 1u;  // the first step builds lists
         FGB_CUDA(cudaMemcpy(b->list_policy.p, init.data(), init.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),

@@ -66,20 +66,21 @@ def test_rows_grow_from_small_capacities_without_changing_results(profile):
 
 @pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
 def test_list_policy_changes_no_result(profile):
-    # the list policy stops building Verlet lists and near rows for a step after one
-    # in which more than 1% of the particles moved over half the skin: every pass then
-    # walks its cells.  A violent scene (a dam break onto a sphere) reaches such steps;
-    # the state after them equals that with lists built every step, bit for bit.
+    # the list policy stops building Verlet lists and near rows when too few particles
+    # of a step could use them: every pass then walks its cells, and walking scenes try
+    # lists again when calm or every 8 steps.  Asked to keep lists only where 95% of a
+    # pass could use them, a dam break onto a sphere switches between the two; the
+    # state equals that with lists built every step, bit for bit.
     params = capi.params(profile, H)
     parts, cfg = scenes.dam_break((20, 16, 20), (2.0, 1.6, 2.0), seed=93, sphere=(1.0, 0.3, 1.0, 0.3))
     out = {}
     for policy in ("1", "0"):
-        os.environ["FGB_LIST_POLICY"] = policy
+        os.environ.update(FGB_LIST_POLICY=policy, FGB_LIST_MIN_USE="95")
         try:
             solver = SphSolver(params=params)
             b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
         finally:
-            del os.environ["FGB_LIST_POLICY"]
+            del os.environ["FGB_LIST_POLICY"], os.environ["FGB_LIST_MIN_USE"]
         off = 0
         for _ in range(40):
             b.step(1)
