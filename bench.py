@@ -807,11 +807,12 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def ncu_case(profile="baseline"):
+def ncu_case(profile="baseline", deep=0):
     """Four plain steps of dam_break_1m (per step: predict, 2 + passes sort kernels,
     reorder, list build, 4 x (lambda, delta), 2 vorticity kernels in the baseline
     profile; colour diffusion instead in the ref profile), then one surface of the
-    256x128x128-cube lattice (position keys, sort, gather, field, scan, emit)."""
+    256x128x128-cube lattice (position keys, sort, gather, field, scan, emit); with
+    deep > 0, `deep` steps before those four (a flow that has broken)."""
     from libfluid_gb300 import build, capi, scenes
     from libfluid_gb300.solver import Batch, SphSolver
     build.build()
@@ -819,6 +820,8 @@ def ncu_case(profile="baseline"):
     parts, cfg = scenes.dam_break_1m()
     solver = SphSolver(params=params)
     batch = Batch(solver, [(parts, cfg)])
+    if deep:
+        batch.step(deep)
     batch.step(4)
     batch.sync()
     tris = batch.surface(0)
@@ -839,13 +842,14 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default launch shapes)")
     ap.add_argument("--serving-log", default=None,
                     help="write the serving leg's tick log (latency, scenes, particles, start) to this .npz")
+    ap.add_argument("--ncu-deep", type=int, default=0, help="steps of --ncu-case before its four")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run 4 untimed steps of the workload and exit (the case that ncu captures)")
     ap.add_argument("--ncu-profile", default="baseline", choices=["baseline", "ref"],
                     help="physics profile of --ncu-case")
     args = ap.parse_args()
     if args.ncu_case:
-        ncu_case(args.ncu_profile)
+        ncu_case(args.ncu_profile, args.ncu_deep)
         return
     if args.warmup < 3:
         args.warmup = 3
