@@ -62,6 +62,17 @@ namespace {
 
 constexpr float kPi = 3.14159265358979323846f;
 
+// Each scene's first triangle after a batched surface: the scanned offset at its
+// first cube (the total for a scene without cubes), gathered for one copy to the host.
+__global__ void k_scene_first_triangles(const SceneDev *__restrict__ scenes, uint32_t n_scenes,
+                                        const uint32_t *__restrict__ offsets, uint64_t cube_total, uint32_t total,
+                                        uint32_t *__restrict__ out) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n_scenes; k += gridDim.x * blockDim.x) {
+        const uint64_t cb = scenes[k].cube_base;
+        out[k] = cb < cube_total ? offsets[cb] : total;
+    }
+}
+
 // Device blocks of one solver's batches, kept for reuse instead of freed.  Every
 // batch of a solver queues its work on the solver's stream, so a block handed back
 // while kernels that use it are still queued can go to the next allocation of the
@@ -535,6 +546,7 @@ struct fgb_batch {
     uint32_t ppt = 1;
     Dev<uint32_t> queue;
     Dev<uint32_t> list_policy;  // per scene: k_list_policy's state
+    Dev<uint32_t> scene_firsts;  // per scene: first triangle of the last batched surface
     uint32_t list_min_use = 25;  // FGB_LIST_MIN_USE: percent of particles using lists that keeps them
     int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
@@ -1804,18 +1816,21 @@ int fgb_batch_surface_all(fgb_batch *b, uint64_t *counts) {
     if (rc) return rc;
     rc = b->surface_emit(t);
     if (rc) return rc;
-    // per-scene triangle ranges: offsets at each scene's first cube
+    // per-scene triangle ranges: offsets at each scene's first cube, gathered on the
+    // device and copied in one piece
     std::vector<uint32_t> firsts(b->n_scenes);
     b->surf_tri_first.assign(b->n_scenes + 1, 0);
     cudaStream_t st = b->stream();
-    for (uint32_t k = 0; k < b->n_scenes; ++k) {
-        const uint64_t cb = b->h_scenes[k].cube_base;
-        if (cb < b->cube_total)
-            FGB_CUDA(cudaMemcpyAsync(&firsts[k], b->offsets.p + cb, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
-                     "surface_all: offsets");
-        else
-            firsts[k] = (uint32_t)t;
+    if (b->scene_firsts.n < b->n_scenes || !b->scene_firsts.p) {
+        PoolScope scope(&b->solver->pool);
+        FGB_CUDA(b->scene_firsts.alloc(b->n_scenes), "surface_all: alloc");
     }
+    k_scene_first_triangles<<<(b->n_scenes + 255) / 256, 256, 0, st>>>(b->d_scenes.p, b->n_scenes, b->offsets.p,
+                                                                       b->cube_total, (uint32_t)t, b->scene_firsts.p);
+    FGB_CUDA(cudaGetLastError(), "surface_all: offsets");
+    FGB_CUDA(cudaMemcpyAsync(firsts.data(), b->scene_firsts.p, b->n_scenes * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             st),
+             "surface_all: offsets");
     FGB_CUDA(cudaStreamSynchronize(st), "surface_all: sync");
     uint32_t f = 0;
     rc = batch_flags_now(b, &f);
