@@ -420,20 +420,29 @@ struct RowWriter {
     uint32_t cap, count = 0;
     uint4 q;
     __device__ __forceinline__ RowWriter(uint32_t *base, uint32_t cap_, uint32_t a)
-        : row(reinterpret_cast<uint4 *>(base + (size_t)a * cap_)), cap(cap_) {}
+        : row(reinterpret_cast<uint4 *>(base + (size_t)a * cap_)), cap(cap_), q(make_uint4(0u, 0u, 0u, 0u)) {}
+    // the last four entries, oldest in x: shifted along on every append and stored
+    // whole when four new ones have come in
     __device__ __forceinline__ void add(uint32_t b) {
-        const uint32_t k = count & 3u;
-        q.x = k == 0 ? b : q.x;
-        q.y = k == 1 ? b : q.y;
-        q.z = k == 2 ? b : q.z;
+        q.x = q.y;
+        q.y = q.z;
+        q.z = q.w;
         q.w = b;
-        if (k == 3 && count < cap) row[count >> 2] = q;
         ++count;
+        if ((count & 3u) == 0 && count <= cap) row[(count >> 2) - 1] = q;
     }
-    // store the last partial vector (its tail entries are stale and never read);
-    // returns the row's count, kListOverflow when it did not fit
+    // store the last partial vector, its entries moved to the front (the tail entries
+    // are stale and never read); returns the row's count, kListOverflow when it did
+    // not fit
     __device__ __forceinline__ uint16_t close() {
-        if ((count & 3u) && count <= cap) row[count >> 2] = q;
+        const uint32_t r = count & 3u;
+        if (r && count <= cap) {
+            uint4 t = q;
+            if (r == 1) t.x = q.w;
+            if (r == 2) t.x = q.z, t.y = q.w;
+            if (r == 3) t.x = q.y, t.y = q.z, t.z = q.w;
+            row[count >> 2] = t;
+        }
         return count > cap ? kListOverflow : (uint16_t)count;
     }
 };
