@@ -1101,6 +1101,13 @@ static int batch_flags_now(fgb_batch *b, uint32_t *f) {
 
 // The per-particle arrays a step rebuilds (sort keys, p*, lists, lambda, ...), for
 // `cap` particles; their contents do not outlive a step.
+// FGB_PACKED=0: the delta and vorticity-apply passes read their neighbours from the
+// separate arrays instead of the packed copies (for comparison; same results)
+static bool packed_off() {
+    const char *e = getenv("FGB_PACKED");
+    return e && strcmp(e, "0") == 0;
+}
+
 static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     PoolScope scope(&b->solver->pool);
     const fgb_params &p = b->solver->params;
@@ -1124,11 +1131,11 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     }
     if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
-    if (!getenv("FGB_NO_PACKED_DELTA")) FGB_CUDA(b->plam.alloc(cap), "batch alloc");
+    if (!packed_off()) FGB_CUDA(b->plam.alloc(cap), "batch alloc");
     FGB_CUDA(b->mass_range.alloc(2), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
     if (p.profile != FGB_PROFILE_REF) {
-        if (!getenv("FGB_NO_PACKED_DELTA")) FGB_CUDA(b->pom.alloc(cap), "batch alloc");
+        if (!packed_off()) FGB_CUDA(b->pom.alloc(cap), "batch alloc");
         FGB_CUDA(b->omega.alloc(cap), "batch alloc");
         FGB_CUDA(b->vx.alloc(cap), "batch alloc");
     } else {

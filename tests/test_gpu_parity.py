@@ -166,6 +166,17 @@ def test_step_parity_sphere_collider(oracle_mod):
     _check_step(oracle_mod, params, parts, cfg, steps=3)
 
 
+def test_step_parity_unequal_masses(oracle_mod):
+    # unequal masses: the baseline's delta and vorticity-apply passes read their
+    # neighbours' masses from the separate arrays (the packed copies need one mass)
+    params = capi.params(capi.PROFILE_BASELINE, H)
+    parts, cfg = scenes.dam_break((20, 16, 20), (2.0, 2.0, 2.0), seed=151)
+    parts["mass"][::7] = np.float32(1.25)
+    parts["mass"][3::11] = np.float32(0.8)
+    parts["type"][::19] = capi.TYPE_OBSTACLE
+    _check_step(oracle_mod, params, parts, cfg, steps=3)
+
+
 def test_step_parity_ref_profile_with_triangles_and_obstacles(oracle_mod):
     params = capi.params(capi.PROFILE_REF, H)
     parts, cfg = scenes.dam_break((16, 16, 16), (2.0, 2.0, 2.0), seed=31)
@@ -415,6 +426,34 @@ def test_persistent_tile_queues_give_the_bits_of_flat_grids(profile, monkeypatch
             for f in ("id", "position", "velocity", "colour"):
                 assert (run[k][f] == out[0][k][f]).all(), (k, f)
     solver.close()
+
+
+@pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
+def test_packed_neighbour_reads_give_the_bits_of_separate_arrays(profile, monkeypatch):
+    # the delta and vorticity-apply passes read neighbours from the lambda and
+    # vorticity passes' packed copies (p* with lambda or |omega| in w) when no
+    # neighbour mass is needed or every mass is equal; FGB_PACKED=0 reads the separate
+    # arrays: the same bits.  (Unequal masses in the baseline profile read the separate
+    # arrays either way; the oracle checks that path, test_step_parity_unequal_masses.)
+    params = capi.params(profile, H)
+    for masses in ("equal", "unequal"):
+        parts, cfg = scenes.dam_break((20, 16, 20), (2.0, 2.0, 2.0), seed=150)
+        parts["type"][::17] = capi.TYPE_OBSTACLE
+        if masses == "unequal":
+            parts["mass"][::7] = np.float32(1.25)
+        solver = SphSolver(params=params)
+        out = []
+        for packed in ("1", "0"):
+            monkeypatch.setenv("FGB_PACKED", packed)
+            b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+            b.step(8)
+            out.append(b.download(0))
+            assert b.error_flags() == 0
+            b.close()
+        monkeypatch.delenv("FGB_PACKED")
+        for f in ("position", "velocity", "colour"):
+            assert (out[0][f] == out[1][f]).all(), (masses, f)
+        solver.close()
 
 
 def test_advance_surface_frames_do_not_change_the_state():
