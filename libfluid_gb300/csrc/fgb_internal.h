@@ -71,8 +71,6 @@ struct StepView {
     // of the step (slots_of_step), ppt particles per thread of a tile
     uint32_t *queue;
     uint32_t ppt;
-    // the order of particles in each window of `block` (k_window_order), null: none
-    uint32_t *perm;
     // {1 while steps build Verlet lists, movers of the step} (null: lists every step)
     uint32_t *list_policy;
     uint32_t list_min_use;  // percent of a pass's particles that keeps lists on

@@ -197,7 +197,6 @@ struct GatherArgs {
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
     uint32_t ppt;
-    const uint32_t *perm;  // null, or the particle each thread takes (k_window_order)
     // null, or per scene: kPolicyWords words of k_list_policy's state
     uint32_t *list_policy;
     int count_lists;  // this lambda pass samples how many particles could use their list
@@ -495,45 +494,6 @@ __device__ __forceinline__ void for_hits(const GatherArgs &A, uint32_t a, const 
     for_row(A.hlist, A.hcap, a, A.hcount[a], sp, f);
 }
 
-// The particle thread t of a gather launch takes: t itself, or its window's order
-// (k_window_order); A.n past the end.
-__device__ __forceinline__ uint32_t particle_of(const GatherArgs &A, uint32_t t) {
-    if (t >= A.n) return A.n;
-    return A.perm ? __ldg(&A.perm[t]) : t;
-}
-
-// The order in which the gathers' threads take the particles of each window of
-// blockDim consecutive sorted particles (one CTA): longest Verlet rows first (a row
-// that overflowed, or a particle that walks, counts as longest), ties in index order.
-// A warp's lanes then loop over rows of similar length instead of waiting on the
-// longest of a spatial mix, and particles never leave their window, so a CTA still
-// covers the same cells.  Every particle's work is unchanged.  Bitonic sort of
-// blockDim (a power of two, at most 256) keys in shared memory.
-__global__ void __launch_bounds__(256) k_window_order(uint32_t n, const uint16_t *__restrict__ ncount,
-                                                     uint32_t *__restrict__ perm) {
-    __shared__ uint32_t key[256];
-    const uint32_t w = blockDim.x, t = threadIdx.x, base = blockIdx.x * w, i = base + t;
-    // (count + 1) << 8 | (255 - t): descending order puts long rows first, then lower
-    // indices; 0 for the slots past the end, which sort last
-    key[t] = i < n ? ((uint32_t)ncount[i] + 1u) << 8 | (255u - t) : 0u;
-    __syncthreads();
-    for (uint32_t k = 2; k <= w; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            const uint32_t p = t ^ j;
-            if (p > t) {
-                const uint32_t a = key[t], b = key[p];
-                const bool desc = (t & k) == 0;
-                if (desc ? a < b : a > b) {
-                    key[t] = b;
-                    key[p] = a;
-                }
-            }
-            __syncthreads();
-        }
-    }
-    if (i < n) perm[i] = base + (255u - (key[t] & 255u));
-}
-
 // The particles of one gather launch, f(a) for each.  Flat: one particle per thread,
 // one CTA per blockDim particles.  Persistent: a grid sized to the GPU whose CTAs take
 // tiles of ppt x blockDim consecutive sorted particles -- a block of cells of one
@@ -543,7 +503,7 @@ __global__ void __launch_bounds__(256) k_window_order(uint32_t n, const uint16_t
 template <bool kTiles, class F>
 __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
     if constexpr (!kTiles) {
-        f(particle_of(A, blockIdx.x * blockDim.x + threadIdx.x));
+        f(blockIdx.x * blockDim.x + threadIdx.x);
         return;
     }
     __shared__ uint32_t s_tile;
@@ -556,7 +516,7 @@ __device__ __forceinline__ void for_tiles(const GatherArgs &A, F &&f) {
         if (base >= A.n) break;
         for (uint32_t k = 0; k < A.ppt; ++k) {
             const uint64_t a = base + (uint64_t)k * blockDim.x + threadIdx.x;
-            f(a < A.n ? particle_of(A, (uint32_t)a) : A.n);  // A.n: past the end, the body returns
+            f(a < A.n ? (uint32_t)a : A.n);  // A.n: past the end, the body returns
         }
     }
 }
@@ -1383,7 +1343,6 @@ GatherArgs gather_args(const StepView &s) {
     A.plam = s.plam;
     A.pom = s.pom;
     A.queue = nullptr;  // per launch, below
-    A.perm = nullptr;   // per launch, below
     A.list_policy = s.cap ? s.list_policy : nullptr;
     A.count_lists = 0;  // the second lambda pass's launch sets it
     A.ppt = s.ppt ? s.ppt : 1;
@@ -1446,7 +1405,6 @@ Launch gather_launch(const StepView &s, uint32_t slot) {
         L.grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(tiles, resident));
         L.A.queue = s.queue + slot;
     }
-    L.A.perm = slot ? s.perm : nullptr;  // the list build (slot 0) orders nothing
     return L;
 }
 
@@ -1477,7 +1435,6 @@ void launch_lambda(const StepView &s, const float4 *ps, int iteration, cudaStrea
     if (iteration == 0 && L.A.cap) {
         if (B.A.queue) k_build_lists<true><<<B.grid, s.block, 0, st>>>(B.A, ps);
         else k_build_lists<false><<<B.grid, s.block, 0, st>>>(B.A, ps);
-        if (s.perm) k_window_order<<<grid_for(s.n, s.block), s.block, 0, st>>>(s.n, s.ncount, s.perm);
         if (ref) run_lambda<FGB_PROFILE_REF, kFresh>(L, s.block, st, ps, s.lambda, s.density);
         else run_lambda<FGB_PROFILE_BASELINE, kFresh>(L, s.block, st, ps, s.lambda, s.density);
     } else if (iteration == 0) {

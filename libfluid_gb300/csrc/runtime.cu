@@ -547,7 +547,6 @@ struct fgb_batch {
     Dev<uint32_t> queue;
     Dev<uint32_t> list_policy;  // per scene: k_list_policy's state
     Dev<uint32_t> scene_firsts;  // per scene: first triangle of the last batched surface
-    Dev<uint32_t> perm;          // the gathers' particle order within each CTA window
     uint32_t list_min_use = 25;  // FGB_LIST_MIN_USE: percent of particles using lists that keeps them
     int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
@@ -650,7 +649,6 @@ struct fgb_batch {
         s.err = err.p;
         s.block = block;
         s.queue = persistent ? queue.p : nullptr;
-        s.perm = nlist.p && list_cap ? perm.p : nullptr;
         s.list_policy = list_policy.p;
         s.list_min_use = list_min_use;
         s.ppt = persistent ? ppt : 1;
@@ -739,7 +737,7 @@ struct fgb_batch {
                 FGB_CUDA(cudaMemsetAsync(cellmax.p, 0, cells_n * sizeof(uint32_t), st), "step: clear cellmax");
             launch_delta(s, pin, pout, (int)it, it + 1 == iterations, st);
             mark(k, st);
-            l += (it == 0 && s.cap) ? (s.perm ? 4 : 3) : 2;
+            l += (it == 0 && s.cap) ? 3 : 2;
             pin = pout;
         }
         if (ph.profile != FGB_PROFILE_REF) {
@@ -1133,8 +1131,6 @@ static int alloc_step_arrays(fgb_batch *b, uint64_t cap) {
     }
     if (b->list_cap && b->hit_cap) FGB_CUDA(b->near.alloc(cap), "batch alloc");
     FGB_CUDA(b->lambda.alloc(cap), "batch alloc");
-    if (b->list_cap && !(getenv("FGB_WINDOW_ORDER") && strcmp(getenv("FGB_WINDOW_ORDER"), "0") == 0))
-        FGB_CUDA(b->perm.alloc(cap), "batch alloc");
     if (!packed_off()) FGB_CUDA(b->plam.alloc(cap), "batch alloc");
     FGB_CUDA(b->mass_range.alloc(2), "batch alloc");
     FGB_CUDA(b->density.alloc(cap), "batch alloc");
