@@ -69,3 +69,30 @@ def test_adapter_matches_c_abi(tmp_path):
     assert got["queries"] == len(results) == 1
     assert (got["q_neighbours"], got["q_colour"]) == (results[0][2], results[0][3])
     solver.close()
+
+
+@pytest.mark.gpu
+def test_dropin_frames_program_matches_c_abi():
+    # bench.py's drop-in leg: tests/cpp/dropin_frames.cpp drives cuda::SphSolver::advance
+    # on a std::vector<fluid::Particle> (baseline profile, sphere collider); its final
+    # positions equal those of fgb_advance on the same scene, frame for frame
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    from libfluid_gb300 import capi, scenes
+    from libfluid_gb300.solver import SphSolver
+    parts, cfg = scenes.dam_break((24, 16, 24), (2.4, 2.0, 2.4), seed=161, sphere=(1.2, 0.3, 1.2, 0.4))
+    got = bench.dropin_frames(scenes.copy_particles(parts), cfg, 2, 3)
+    assert "pos_checksum" in got, got
+    solver = SphSolver(params=capi.params(capi.PROFILE_BASELINE, 0.1))
+    state = scenes.copy_particles(parts)
+    cfg.surface = 0
+    for _ in range(5):
+        solver.advance(cfg, state)
+    solver.close()
+    p = state["position"].reshape(-1, 3).astype(np.float32).astype(np.float64)
+    want = 0.0
+    for x, y, z in p:  # the program's order of summation
+        want += x + 2.0 * y + 3.0 * z
+    assert got["n"] == len(parts["mass"])
+    assert got["pos_checksum"] == pytest.approx(want, rel=1e-9)
