@@ -95,4 +95,4 @@ def test_dropin_frames_program_matches_c_abi():
     for x, y, z in p:  # the program's order of summation
         want += x + 2.0 * y + 3.0 * z
     assert got["n"] == len(parts["mass"])
-    assert got["pos_checksum"] == pytest.approx(want, rel=1e-9)
+    assert got["pos_checksum"] == pytest.approx(want, rel=1e-8)  # printed to 9 digits
