@@ -581,7 +581,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * total / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "dam_break_1m", "particles": n, "iterations": 4, "parallelism": "cpu"},
+        # the same keys as our arm's config; the reference's CPU solver has no sphere
+        # collider and no L2 to flush
+        "config": {"workload": "dam_break_1m", "particles": n, "iterations": 4, "sphere_collider": False,
+                   "l2": "not applicable (CPU)", "parallelism": f"cpu x{cores} threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": note,
@@ -772,11 +775,12 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "dam_break_1m", "particles": n, "iterations": int(cfg.iterations),
                        "sphere_collider": True, "l2": "flushed (256 MiB write) before every timed step",
-                       "parallelism": f"replicas x{world}", "cuda_graph": True,
-                       "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
-                                      "persistent": bool(tuned.persistent),
-                                      "particles_per_thread": int(tuned.particles_per_thread),
-                                      "trial_steps": int(tuned.steps)} if tuned else None)},
+                       "parallelism": f"replicas x{world}"},
+            "setup": {"cuda_graph": True,
+                      "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
+                                     "persistent": bool(tuned.persistent),
+                                     "particles_per_thread": int(tuned.particles_per_thread),
+                                     "trial_steps": int(tuned.steps)} if tuned else None)},
             # direct: kernels read id/type/mass/colour/position/velocity (44 B) from the
             # caller's arrays and write them back; staged: pinned float4 x, float4 v,
             # type, colour up (40 B), the same plus the upload slot down (44 B)
