@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -99,6 +100,7 @@ struct fgb_server {
     // worker-only state
     std::vector<std::unique_ptr<ServeGroup>> groups;
     size_t next_group = 0;  // round-robin position
+    double spread = 1.0;    // largest group / smallest group kept without re-spreading
     std::thread worker;
     // statistics (under mu)
     uint64_t ticks = 0, particle_steps = 0, completed = 0, rejected = 0, failed = 0, rebuilds = 0;
@@ -178,7 +180,9 @@ struct fgb_server {
             }
         if (used.size() < 2) return;
         const uint64_t need = (total + opt.tick_particles - 1) / opt.tick_particles;
-        if (used.size() <= need && hi == lo) return;
+        // groups as few as the particles need, and within `spread` of each other: keep
+        // them (every change of membership is a rebuild)
+        if (used.size() <= need && (double)hi <= spread * (double)lo) return;
         // LPT: largest scene first, onto the lightest group it fits
         std::vector<Request *> all;
         for (ServeGroup *g : used) all.insert(all.end(), g->want.begin(), g->want.end());
@@ -463,6 +467,7 @@ int fgb_serve_create(fgb_solver *s, const fgb_serve_options *opt, fgb_server **o
     if (!sv->opt.max_active) sv->opt.max_active = 256;
     if (!sv->opt.tick_particles) sv->opt.tick_particles = 2097152;
     if (!sv->opt.max_steps_per_tick) sv->opt.max_steps_per_tick = 16;
+    if (const char *e = getenv("FGB_SERVE_SPREAD")) sv->spread = std::max(1.0, atof(e));
     cudaGetDevice(&sv->device);
     sv->t0 = now_s();
     sv->worker = std::thread([sv] { sv->run(); });
