@@ -9,9 +9,10 @@
 // group is small (tick_steps).  A tick's latency is linear in its particle-steps
 // (~0.3 ms + 3.2 ns a particle-step on GB300), so the groups are
 // kept as few and as even as the scenes allow: a new scene joins the lightest group
-// it fits, and whenever the groups are uneven (or more than ceil(total /
-// tick_particles) of them exist) the scenes are re-spread largest first onto the
-// lightest group (LPT); a group that ends up with the same scenes keeps its batch.  When a group's membership changes,
+// it fits, and whenever the largest group holds more than 1.5x the smallest (or more
+// than ceil(total / tick_particles) groups exist) the scenes are re-spread largest
+// first onto the lightest group (LPT); a group that ends up with the same scenes keeps
+// its batch.  When a group's membership changes,
 // its scenes are copied device-to-device into a new batch from wherever they live
 // (fgb_batch_copy_scene keeps their particle order, so a scene's result is
 // bit-identical alone and in any mix).  Finished scenes optionally run marching
@@ -100,7 +101,7 @@ struct fgb_server {
     // worker-only state
     std::vector<std::unique_ptr<ServeGroup>> groups;
     size_t next_group = 0;  // round-robin position
-    double spread = 1.0;    // largest group / smallest group kept without re-spreading
+    double spread = 1.5;    // largest group / smallest group kept without re-spreading
     std::thread worker;
     // statistics (under mu)
     uint64_t ticks = 0, particle_steps = 0, completed = 0, rejected = 0, failed = 0, rebuilds = 0;
