@@ -1055,7 +1055,9 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
     }
     const float gs = ph.spikyf * ph.inv_rho0;
     const float ws = ph.poly6f * ph.inv_rho0;
-    const float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;
+    // omega = sum_b m_b / rho0 (v_b - v_a) x grad_b W(x_a - x_b), and grad_b W = -grad_a W
+    // = -spikyf (h - r)^2 d / r: the sum o carries grad_a's factor, so its sign flips
+    const float ox = -(o[0] * gs), oy = -(o[1] * gs), oz = -(o[2] * gs);
     const float om = sqrtf(ox * ox + oy * oy + oz * oz);
     omega[a] = make_float4(ox, oy, oz, om);
     if (A.pom) A.pom[a] = make_float4(pa.x, pa.y, pa.z, om);

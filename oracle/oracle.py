@@ -228,7 +228,8 @@ class Lattice(ctypes.Structure):
 
 class Probe(ctypes.Structure):
     _fields_ = [("keys", ctypes.c_void_p), ("order", ctypes.c_void_p), ("cells", ctypes.c_void_p),
-                ("lambda_", ctypes.c_void_p), ("density", ctypes.c_void_p), ("pstar", ctypes.c_void_p)]
+                ("lambda_", ctypes.c_void_p), ("density", ctypes.c_void_p), ("pstar", ctypes.c_void_p),
+                ("omega", ctypes.c_void_p)]
 
 
 def _ptr(a):
@@ -271,9 +272,10 @@ def step(params, cfg, parts, colliders=None, probe=False):
             "lambda": np.zeros(n, np.float32),
             "density": np.zeros(n, np.float32),
             "pstar": np.zeros(3 * n, np.float32),
+            "omega": np.zeros(4 * n, np.float32),
         }
         pr = Probe(_ptr(out["keys"]), _ptr(out["order"]), _ptr(out["cells"]), _ptr(out["lambda"]),
-                   _ptr(out["density"]), _ptr(out["pstar"]))
+                   _ptr(out["density"]), _ptr(out["pstar"]), _ptr(out["omega"]))
     tris = None
     ntris = 0
     if colliders is not None and len(colliders):

@@ -559,7 +559,7 @@ static inline void cross3(const float *a, const float *b, float *o) {
 /* Baseline velocity terms (PBF paper eq. 15-17): omega and XSPH, then the
  * vorticity-confinement force.  Sums over fluid neighbours, SPH-normalised with
  * m_j / rho0. */
-static void velocity_terms(const state *s, const float *ps, float *vel) {
+static void velocity_terms(const state *s, const float *ps, float *vel, float *omega_out) {
     const kc *k = &s->k;
     const size_t n = s->n;
     const float gs = k->spikyf * k->inv_rho0;
@@ -603,7 +603,9 @@ static void velocity_terms(const state *s, const float *ps, float *vel) {
                 }
             }
         }
-        float ox = o[0] * gs, oy = o[1] * gs, oz = o[2] * gs;
+        /* omega = sum_b m_b / rho0 (v_b - v_a) x grad_b W(x_a - x_b) (PBF paper eq. 15),
+         * grad_b W = -grad_a W = -spikyf (h - r)^2 d / r */
+        float ox = -(o[0] * gs), oy = -(o[1] * gs), oz = -(o[2] * gs);
         om[4 * a] = ox;
         om[4 * a + 1] = oy;
         om[4 * a + 2] = oz;
@@ -650,6 +652,7 @@ static void velocity_terms(const state *s, const float *ps, float *vel) {
         vel[3 * a + 1] = fmaf(dt, f[1] * ve, vx[3 * a + 1]);
         vel[3 * a + 2] = fmaf(dt, f[2] * ve, vx[3 * a + 2]);
     }
+    if (omega_out) memcpy(omega_out, om, 4 * n * sizeof(float));
     free(om);
     free(vx);
 }
@@ -749,7 +752,7 @@ int orc_step(const fgb_params *p, const fgb_config *c, size_t n, uint64_t *id, i
                 vel[3 * i + a] = dx * inv_dt;
             }
         }
-        velocity_terms(&s, ps, vel);
+        velocity_terms(&s, ps, vel, probe ? probe->omega : NULL);
 #pragma omp parallel for schedule(static)
         for (long i = 0; i < (long)n; ++i) {
             if (type[i] == FGB_TYPE_OBSTACLE) continue;

@@ -49,6 +49,7 @@ typedef struct orc_probe {
     float *lambda;      /* n, last iteration */
     float *density;     /* n, last iteration */
     float *pstar;       /* 3n, predicted p* in sorted order, before the solver iterations */
+    float *omega;       /* 4n, vorticity (xyz, |omega|) in sorted order (baseline profile) */
 } orc_probe;
 
 uint32_t orc_morton(uint32_t x, uint32_t y, uint32_t z);
