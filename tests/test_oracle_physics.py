@@ -97,3 +97,21 @@ def test_vorticity_confinement_feeds_the_rotation(orc):
         vq = q["velocity"].reshape(-1, 3)
         ang.append(float((x[:, 2] * vq[:, 0] - x[:, 0] * vq[:, 2]).sum()))  # L_y
     assert 0 < ang[0] < ang[1] < ang[2], ang
+
+
+def test_xsph_smooths_velocity_noise(orc):
+    # XSPH adds c sum m_b/rho0 (v_b - v_a) W_ab: a smoothing of the velocity field, so
+    # noise on a cube at rest leaves the step with less velocity variance the larger c is
+    parts, cfg = _cube()
+    rng = np.random.default_rng(3)
+    parts["velocity"][:] = (0.05 * rng.standard_normal(parts["velocity"].shape)).astype(np.float32)
+    var = []
+    for c in (0.0, 0.05, 0.2):
+        pc = capi.params(capi.PROFILE_BASELINE, H)
+        pc.xsph_c = c
+        pc.vorticity_epsilon = 0.0
+        q = scenes.copy_particles(parts)
+        orc.step(pc, cfg, q)
+        v = q["velocity"].reshape(-1, 3).astype(np.float64)
+        var.append(float(((v - v.mean(0)) ** 2).sum(1).mean()))
+    assert var[0] > var[1] > var[2], var
