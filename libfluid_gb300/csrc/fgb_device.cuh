@@ -96,9 +96,20 @@ struct SceneDev {
     float lat_step;
     float resolution;
     float iso;
+    float mc_r2_lt;      // ref profile: sqrtf(r2) < h * scale exactly when r2 < mc_r2_lt
     uint64_t lat_base;   // first lattice sample of this scene
     uint64_t cube_base;  // first cube of this scene
+    uint64_t brick_base; // first field brick (kBrick* samples) of this scene
 };
+
+// The field kernel's bricks: one CTA samples a 4 x 8 x 8 block of lattice nodes, each
+// warp a 2 x 4 x 4 block of it, so that a warp's lanes share their grid cells.
+constexpr uint32_t kBrickX = 4, kBrickY = 8, kBrickZ = 8;
+__host__ __device__ inline uint64_t field_bricks(const uint32_t *lat) {
+    if (!lat[0] || !lat[1] || !lat[2]) return 0;
+    return (uint64_t)((lat[0] + kBrickX - 1) / kBrickX) * ((lat[1] + kBrickY - 1) / kBrickY) *
+           ((lat[2] + kBrickZ - 1) / kBrickZ);
+}
 
 struct WellDev {
     float centre[3];

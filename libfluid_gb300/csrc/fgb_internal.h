@@ -243,7 +243,7 @@ struct SurfaceView {
     uint8_t *cases;
     uint32_t *offsets;
     uint32_t *total;         // device, one u32
-    uint64_t lat_begin, lat_end, cube_begin, cube_end;
+    uint64_t lat_begin, lat_end, cube_begin, cube_end, brick_begin, brick_end;
     void *scan_scratch;
     uint64_t scan_scratch_bytes;
     uint32_t *err;

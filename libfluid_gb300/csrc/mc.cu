@@ -8,6 +8,7 @@
 // cube-major order with each cube's triangles in table order -- the order of the
 // reference's CPU marchSingle loop (surface.hpp:185-266), whose edge lerp with its
 // 1e-5 snapping (surface.hpp:47-53) is what the emit kernel evaluates.
+#include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -36,12 +37,15 @@ __constant__ uint8_t c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0
 __constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
                                       {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 
-// Scene owning a global lattice sample / cube (scenes sorted by base).
-__device__ __forceinline__ uint32_t find_scene(const SceneDev *scenes, uint32_t lo, uint32_t hi, uint64_t q,
-                                               bool cubes) {
+// Scene owning a global lattice sample, cube or field brick (scenes sorted by base).
+enum class Base { kSample, kCube, kBrick };
+
+template <Base B>
+__device__ __forceinline__ uint32_t find_scene(const SceneDev *scenes, uint32_t lo, uint32_t hi, uint64_t q) {
     while (hi - lo > 1) {
         uint32_t mid = (lo + hi) >> 1;
-        uint64_t base = cubes ? scenes[mid].cube_base : scenes[mid].lat_base;
+        const SceneDev &S = scenes[mid];
+        const uint64_t base = B == Base::kCube ? S.cube_base : B == Base::kBrick ? S.brick_base : S.lat_base;
         if (base <= q) lo = mid;
         else hi = mid;
     }
@@ -61,20 +65,108 @@ __device__ __forceinline__ uint32_t argb_pack(const float *ch) {
     return out;
 }
 
+// The particles of the 27 cells around (cx, cy, cz) in walk order as f(b, x_b), with
+// the positions of a cell's candidates loaded four at a time ahead of the tests.
+template <class F>
+__device__ __forceinline__ void field_walk(const SceneDev &S, const uint2 *__restrict__ cells,
+                                           const float4 *__restrict__ xs, int cx, int cy, int cz, F &&f) {
+    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+    const uint2 *tbl = cells + S.table_base;
+    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z > ez) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = cy + dy;
+            if (y < 0 || y > ey) continue;
+            const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
+            for (int x = x0; x <= x1; ++x) {
+                const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
+                uint32_t b = c.x;
+                for (; b + 4 <= c.y; b += 4) {
+                    const float4 p0 = __ldg(&xs[b]), p1 = __ldg(&xs[b + 1]), p2 = __ldg(&xs[b + 2]),
+                                 p3 = __ldg(&xs[b + 3]);
+                    f(b, p0);
+                    f(b + 1, p1);
+                    f(b + 2, p2);
+                    f(b + 3, p3);
+                }
+                for (; b < c.y; ++b) f(b, __ldg(&xs[b]));
+            }
+        }
+    }
+}
+
+// Field value, normal and colour sums of one lattice node over its 27 cells.  kUnit:
+// the scene's scale is 1, so x_b / scale is x_b itself and the divisions are skipped
+// (the same values).  The range test comes before the obstacle test (both must pass)
+// so that only candidates in range load their type.
+template <int PROFILE, bool kUnit>
+__device__ __forceinline__ void field_sums(const SceneDev &S, const Phys &ph, const uint2 *__restrict__ cells,
+                                           const float4 *__restrict__ xs, const int32_t *__restrict__ type,
+                                           const uint32_t *__restrict__ col, const int *cc, const float *node,
+                                           float *acc, uint32_t *cl, uint32_t &N) {
+    const float aw[3] = {node[0] * S.scale, node[1] * S.scale, node[2] * S.scale};
+    float v = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    field_walk(S, cells, xs, cc[0], cc[1], cc[2], [&](uint32_t b, const float4 &xb) {
+        if (PROFILE == FGB_PROFILE_REF) {
+            const float lx = xb.x - aw[0], ly = xb.y - aw[1], lz = xb.z - aw[2];
+            const float r2 = lx * lx + ly * ly + lz * lz;
+            if (!(r2 < S.mc_r2_lt)) return;  // sqrtf(r2) >= h * scale
+            if (S.obstacles && __ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
+            const float len = sqrtf(r2);
+            const float den = (ph.mc_infl == 0.5f) ? sqrtf(len) : powf(len, ph.mc_infl);
+            const float sc = (-ph.mc_infl * ph.mc_size) / den;
+            nx = __fmaf_rn(sc, lx, nx);
+            ny = __fmaf_rn(sc, ly, ny);
+            nz = __fmaf_rn(sc, lz, nz);
+            v = v + ph.mc_size / den;
+        } else {
+            float ax, ay, az;
+            if (kUnit) ax = xb.x, ay = xb.y, az = xb.z;
+            else ax = xb.x / S.scale, ay = xb.y / S.scale, az = xb.z / S.scale;
+            const float dx = node[0] - ax, dy = node[1] - ay, dz = node[2] - az;
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (!(r2 <= ph.hh)) return;
+            if (S.obstacles && __ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
+            const float t = ph.hh - r2;
+            const float mt = xb.w * (t * t);
+            v = __fmaf_rn(mt, t, v);
+            nx = __fmaf_rn(mt, dx, nx);
+            ny = __fmaf_rn(mt, dy, ny);
+            nz = __fmaf_rn(mt, dz, nz);
+        }
+        const uint32_t c = __ldg(&col[b]);
+        for (int ch = 0; ch < 4; ++ch) cl[ch] += argb_channel(c, ch);
+        N++;
+    });
+    acc[0] = v;
+    acc[1] = nx;
+    acc[2] = ny;
+    acc[3] = nz;
+}
+
+// One CTA per brick of kBrickX x kBrickY x kBrickZ lattice nodes of one scene; every
+// node's value is its own walk's, whatever the thread that computes it.
 template <int PROFILE>
 __global__ void __launch_bounds__(256)
     k_field(const SceneDev *__restrict__ scenes, uint32_t scene_begin, uint32_t scene_end, Phys ph,
             const uint2 *__restrict__ cells, const float4 *__restrict__ xs, const int32_t *__restrict__ type,
-            const uint32_t *__restrict__ col, uint64_t lat_begin, uint64_t lat_end, float4 *__restrict__ lattice,
+            const uint32_t *__restrict__ col, uint64_t brick_begin, float4 *__restrict__ lattice,
             uint32_t *__restrict__ lattice_col) {
-    const uint64_t q = lat_begin + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= lat_end) return;
-    const uint32_t s = find_scene(scenes, scene_begin, scene_end, q, false);
+    const uint64_t brick = brick_begin + blockIdx.x;
+    const uint32_t s = find_scene<Base::kBrick>(scenes, scene_begin, scene_end, brick);
     const SceneDev &S = scenes[s];
-    const uint64_t local = q - S.lat_base;
-    const uint64_t sy = S.lat[1], sz = S.lat[2];
-    const uint32_t ix = (uint32_t)(local / (sy * sz)), iy = (uint32_t)((local / sz) % sy),
-                   iz = (uint32_t)(local % sz);
+    const uint64_t local = brick - S.brick_base;
+    const uint64_t nby = (S.lat[1] + kBrickY - 1) / kBrickY, nbz = (S.lat[2] + kBrickZ - 1) / kBrickZ;
+    const uint32_t bz = (uint32_t)(local % nbz), by = (uint32_t)((local / nbz) % nby),
+                   bx = (uint32_t)(local / (nbz * nby));
+    const uint32_t w = threadIdx.x >> 5, l = threadIdx.x & 31u;
+    const uint32_t ix = bx * kBrickX + (w & 1u) * 2u + (l & 1u);
+    const uint32_t iy = by * kBrickY + ((w >> 1) & 1u) * 4u + ((l >> 1) & 3u);
+    const uint32_t iz = bz * kBrickZ + (w >> 2) * 4u + (l >> 3);
+    if (ix >= S.lat[0] || iy >= S.lat[1] || iz >= S.lat[2]) return;
+    const uint64_t q = S.lat_base + ((uint64_t)ix * S.lat[1] + iy) * S.lat[2] + iz;
     const float node[3] = {S.lat_origin[0] + (float)ix * S.lat_step, S.lat_origin[1] + (float)iy * S.lat_step,
                            S.lat_origin[2] + (float)iz * S.lat_step};
     int cc[3];
@@ -87,40 +179,13 @@ __global__ void __launch_bounds__(256)
     } else {
         for (int a = 0; a < 3; ++a) cc[a] = (int)quantise(node[a], S.min_ext[a], ph.h, S.ext[a]);
     }
-    const float thr = ph.h * S.scale;
-    const float aw[3] = {node[0] * S.scale, node[1] * S.scale, node[2] * S.scale};
-    float v = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
+    float acc[4];
     // channel sums as integers: below 2^24, so equal to the float sums in any order
     uint32_t cl[4] = {0, 0, 0, 0};
     uint32_t N = 0;
-    for_neighbour_cells(S, cells, cc[0], cc[1], cc[2], [&](uint32_t b) {
-        if (S.obstacles && __ldg(&type[b]) == FGB_TYPE_OBSTACLE) return;
-        const float4 xb = __ldg(&xs[b]);
-        if (PROFILE == FGB_PROFILE_REF) {
-            const float lx = xb.x - aw[0], ly = xb.y - aw[1], lz = xb.z - aw[2];
-            const float len = sqrtf(lx * lx + ly * ly + lz * lz);
-            if (!(len < thr)) return;
-            const float den = (ph.mc_infl == 0.5f) ? sqrtf(len) : powf(len, ph.mc_infl);
-            const float sc = (-ph.mc_infl * ph.mc_size) / den;
-            nx = __fmaf_rn(sc, lx, nx);
-            ny = __fmaf_rn(sc, ly, ny);
-            nz = __fmaf_rn(sc, lz, nz);
-            v = v + ph.mc_size / den;
-        } else {
-            const float dx = node[0] - xb.x / S.scale, dy = node[1] - xb.y / S.scale, dz = node[2] - xb.z / S.scale;
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (!(r2 <= ph.hh)) return;
-            const float t = ph.hh - r2;
-            const float mt = xb.w * (t * t);
-            v = __fmaf_rn(mt, t, v);
-            nx = __fmaf_rn(mt, dx, nx);
-            ny = __fmaf_rn(mt, dy, ny);
-            nz = __fmaf_rn(mt, dz, nz);
-        }
-        const uint32_t c = __ldg(&col[b]);
-        for (int ch = 0; ch < 4; ++ch) cl[ch] += argb_channel(c, ch);
-        N++;
-    });
+    if (S.scale == 1.f) field_sums<PROFILE, true>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
+    else field_sums<PROFILE, false>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
+    float v = acc[0], nx = acc[1], ny = acc[2], nz = acc[3];
     if (PROFILE != FGB_PROFILE_REF) v = v * ph.poly6f;
     const float nl = sqrtf(nx * nx + ny * ny + nz * nz);
     if (nl > 0.f) {
@@ -144,7 +209,7 @@ struct CubeCount {
     uint64_t cube_begin;
     __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
         const uint64_t q = cube_begin + i;
-        const uint32_t s = find_scene(scenes, scene_begin, scene_end, q, true);
+        const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
         const SceneDev &S = scenes[s];
         const uint64_t local = q - S.cube_base;
         const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
@@ -162,10 +227,13 @@ struct CubeCount {
     }
 };
 
-__device__ __forceinline__ int snap_select(float iso, float v1, float v2) {
-    if ((double)fabsf(iso - v1) < 0.00001) return 1;
-    if ((double)fabsf(iso - v2) < 0.00001) return 2;
-    if ((double)fabsf(v1 - v2) < 0.00001) return 1;
+// surface.hpp:47-53 compares |d| (a float widened to double) with the double 0.00001;
+// `snap` is the smallest float not below that double, so |d| < snap is the same test
+// without double arithmetic.
+__device__ __forceinline__ int snap_select(float iso, float v1, float v2, float snap) {
+    if (fabsf(iso - v1) < snap) return 1;
+    if (fabsf(iso - v2) < snap) return 2;
+    if (fabsf(v1 - v2) < snap) return 1;
     return 0;
 }
 
@@ -173,7 +241,7 @@ __global__ void __launch_bounds__(256)
     k_emit(const SceneDev *__restrict__ scenes, uint32_t scene_begin, uint32_t scene_end,
            const float4 *__restrict__ lattice, const uint32_t *__restrict__ lattice_col,
            const uint8_t *__restrict__ cases, const uint32_t *__restrict__ offsets, uint64_t cube_begin,
-           uint64_t cubes, fgb_mesh_triangle *__restrict__ out, uint64_t cap, uint32_t *err) {
+           uint64_t cubes, fgb_mesh_triangle *__restrict__ out, uint64_t cap, float snap, uint32_t *err) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cubes) return;
     const uint32_t ci = cases[i];
@@ -185,7 +253,7 @@ __global__ void __launch_bounds__(256)
         return;
     }
     const uint64_t q = cube_begin + i;
-    const uint32_t s = find_scene(scenes, scene_begin, scene_end, q, true);
+    const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
     const SceneDev &S = scenes[s];
     const uint64_t local = q - S.cube_base;
     const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
@@ -215,7 +283,7 @@ __global__ void __launch_bounds__(256)
     for (int e = 0; e < 12; ++e) {
         if (!(em & (1u << e))) continue;
         const int a = c_edge[e][0], b = c_edge[e][1];
-        const int sel = snap_select(iso, val[a], val[b]);
+        const int sel = snap_select(iso, val[a], val[b], snap);
         if (sel) {
             const int k = sel == 1 ? a : b;
             for (int d = 0; d < 3; ++d) {
@@ -255,16 +323,16 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 cudaError_t launch_surface_count(const SurfaceView &v, cudaStream_t st, uint64_t *launches) {
-    const uint64_t samples = v.lat_end - v.lat_begin;
-    if (samples) {
-        const unsigned grid = (unsigned)((samples + 255) / 256);
+    const uint64_t bricks = v.brick_end - v.brick_begin;
+    if (bricks) {
+        const unsigned grid = (unsigned)bricks;
         if (v.ph.profile == FGB_PROFILE_REF)
             k_field<FGB_PROFILE_REF><<<grid, 256, 0, st>>>(v.scenes, v.scene_begin, v.scene_end, v.ph, v.cells, v.xs,
-                                                          v.type, v.col, v.lat_begin, v.lat_end, v.lattice,
+                                                          v.type, v.col, v.brick_begin, v.lattice,
                                                           v.lattice_col);
         else
             k_field<FGB_PROFILE_BASELINE><<<grid, 256, 0, st>>>(v.scenes, v.scene_begin, v.scene_end, v.ph, v.cells,
-                                                               v.xs, v.type, v.col, v.lat_begin, v.lat_end,
+                                                               v.xs, v.type, v.col, v.brick_begin,
                                                                v.lattice, v.lattice_col);
         if (launches) *launches += 1;
     }
@@ -273,13 +341,21 @@ cudaError_t launch_surface_count(const SurfaceView &v, cudaStream_t st, uint64_t
                        st, v.err, launches);
 }
 
+// The smallest float whose widening to double is not below 0.00001.
+static float snap_threshold() {
+    float f = (float)0.00001;
+    while ((double)f < 0.00001) f = std::nextafter(f, INFINITY);
+    while ((double)std::nextafter(f, 0.f) >= 0.00001) f = std::nextafter(f, 0.f);
+    return f;
+}
+
 cudaError_t launch_surface_emit(const SurfaceView &v, fgb_mesh_triangle *out, uint64_t cap, cudaStream_t st,
                                 uint64_t *launches) {
     const uint64_t cubes = v.cube_end - v.cube_begin;
     if (!cubes || !cap) return cudaSuccess;
     k_emit<<<(unsigned)((cubes + 255) / 256), 256, 0, st>>>(v.scenes, v.scene_begin, v.scene_end, v.lattice,
                                                            v.lattice_col, v.cases, v.offsets, v.cube_begin, cubes,
-                                                           out, cap, v.err);
+                                                           out, cap, snap_threshold(), v.err);
     if (launches) *launches += 1;
     return cudaGetLastError();
 }

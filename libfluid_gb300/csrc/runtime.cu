@@ -18,6 +18,7 @@
 //         sample, case u8 + offset u32 per cube, triangles
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstdio>
 #include <cstring>
 #include <atomic>
@@ -243,6 +244,19 @@ Phys make_phys(const fgb_params &p) {
 }
 
 // Grid and lattice geometry of one scene (same float operations as the oracle).
+// The smallest float T with sqrtf(T) >= thr, so that sqrtf(r2) < thr exactly when
+// r2 < T (sqrtf is correctly rounded and monotonic): range tests against a length
+// then need no square root.
+float sqrt_lt_bound(float thr) {
+    if (!(thr > 0.f)) return 0.f;  // no r2 has sqrtf(r2) < thr
+    if (std::isinf(thr)) return thr;
+    float x = thr * thr;
+    if (std::isinf(x)) x = std::numeric_limits<float>::max();
+    while (x > 0.f && std::sqrt(std::nextafter(x, 0.f)) >= thr) x = std::nextafter(x, 0.f);
+    while (std::sqrt(x) < thr) x = std::nextafter(x, INFINITY);
+    return x;
+}
+
 void scene_geometry(const fgb_params &p, const fgb_config &c, SceneDev &S) {
     const float pad = p.h * 2.f;
     for (int a = 0; a < 3; ++a) {
@@ -266,6 +280,7 @@ void scene_geometry(const fgb_params &p, const fgb_config &c, SceneDev &S) {
     for (int a = 0; a < 4; ++a) S.sphere[a] = c.sphere[a];
     S.resolution = c.resolution;
     S.iso = c.isolevel;
+    S.mc_r2_lt = sqrt_lt_bound(p.h * c.scale);
     const float step = c.resolution > 0.f ? p.h / c.resolution : 0.f;
     S.lat_step = step;
     for (int a = 0; a < 3; ++a) {
@@ -567,7 +582,7 @@ struct fgb_batch {
     Dev<uint32_t> q_out;
     // surface
     bool surf_ready = false;
-    uint64_t lat_total = 0, cube_total = 0;
+    uint64_t lat_total = 0, cube_total = 0, brick_total = 0;
     Dev<uint32_t> mc_keys, mc_vals;
     Dev<float4> mc_xs;
     Dev<int32_t> mc_type;
@@ -1034,6 +1049,8 @@ struct fgb_batch {
         v.lat_end = (e < n_scenes) ? h_scenes[e].lat_base : lat_total;
         v.cube_begin = h_scenes[b].cube_base;
         v.cube_end = (e < n_scenes) ? h_scenes[e].cube_base : cube_total;
+        v.brick_begin = h_scenes[b].brick_base;
+        v.brick_end = (e < n_scenes) ? h_scenes[e].brick_base : brick_total;
         v.scan_scratch = scan_scratch.p;
         v.scan_scratch_bytes = scan_scratch_bytes;
         v.err = err.p;
@@ -1171,7 +1188,7 @@ static int batch_init(fgb_batch *b) {
     b->ph = s->ph;
     b->h_scenes.assign(b->n_scenes, SceneDev{});
     uint32_t max_ext = 0;
-    uint64_t table = 0, lat = 0, cubes = 0;
+    uint64_t table = 0, lat = 0, cubes = 0, bricks = 0;
     std::vector<WellDev> wells;
     b->first.resize(b->n_scenes);
     uint64_t off = 0;
@@ -1203,6 +1220,8 @@ static int batch_init(fgb_batch *b) {
         }
         S.lat_base = lat;
         S.cube_base = cubes;
+        S.brick_base = bricks;
+        bricks += field_bricks(S.lat);
         lat += (uint64_t)S.lat[0] * S.lat[1] * S.lat[2];
         if (S.lat[0] > 1 && S.lat[1] > 1 && S.lat[2] > 1)
             cubes += (uint64_t)(S.lat[0] - 1) * (S.lat[1] - 1) * (S.lat[2] - 1);
@@ -1214,6 +1233,7 @@ static int batch_init(fgb_batch *b) {
     b->cells_n = table;
     b->lat_total = lat;
     b->cube_total = cubes;
+    b->brick_total = bricks;
     if (cubes > 0xffffffffull) return fail(FGB_ERR_CAPACITY, "batch: more than 2^32-1 marching cubes");
     b->mbits = 3 * bits_for(max_ext);
     b->sbits = bits_for(b->n_scenes - 1);
