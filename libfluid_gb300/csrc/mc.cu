@@ -32,11 +32,6 @@ void mc_tables_upload() {
 
 namespace {
 
-__constant__ uint8_t c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
-                                       {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-__constant__ uint8_t c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
-                                      {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-
 // Scene owning a global lattice sample, cube or field brick (scenes sorted by base).
 enum class Base { kSample, kCube, kBrick };
 
@@ -200,30 +195,65 @@ __global__ void __launch_bounds__(256)
     lattice_col[q] = argb_pack(avg);
 }
 
-// Scan loader: classify cube `cube_begin + i`, record its case, return its triangles.
+// Scan loader: classify cubes `cube_begin + i`, record their cases, return their
+// triangle counts.
 struct CubeCount {
     const SceneDev *scenes;
     uint32_t scene_begin, scene_end;
     const float4 *lattice;
     uint8_t *cases;
     uint64_t cube_begin;
-    __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
-        const uint64_t q = cube_begin + i;
-        const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
-        const SceneDev &S = scenes[s];
-        const uint64_t local = q - S.cube_base;
-        const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
-        const uint64_t x = local / (my * mz), y = (local / mz) % my, z = local % mz;
-        const uint64_t sy = S.lat[1], sz = S.lat[2];
-        uint32_t ci = 0;
+    // Cubes first .. first + K - 1 (those below n): the scene and the cube's
+    // coordinates are found once and then stepped, and a cube that follows another
+    // along z takes its four corners on the plane between them from that cube's case,
+    // loading four lattice values instead of eight.
+    template <int K>
+    __device__ __forceinline__ void run(uint64_t first, uint64_t n, uint32_t (&v)[K]) const {
+        const SceneDev *S = nullptr;
+        uint64_t row = 0, plane = 0;  // lattice index of (x, y, 0); samples per x-plane
+        uint32_t sz = 0, mx = 0, my = 0, mz = 0, x = 0, y = 0, z = 0, prev = 0;
+        bool have = false;
+        float iso = 0.f;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const uint64_t idx = S.lat_base + ((x + c_corner[c][0]) * sy + (y + c_corner[c][1])) * sz +
-                                 (z + c_corner[c][2]);
-            if (__ldg(&lattice[idx].x) < S.iso) ci |= 1u << c;
+        for (int k = 0; k < K; ++k) {
+            v[k] = 0u;
+            const uint64_t i = first + k;
+            if (i >= n) continue;
+            if (!S || x >= mx) {  // first cube, or past the end of a scene's cubes
+                const uint64_t q = cube_begin + i;
+                S = &scenes[find_scene<Base::kCube>(scenes, scene_begin, scene_end, q)];
+                const uint64_t local = q - S->cube_base;
+                mx = S->lat[0] - 1;
+                my = S->lat[1] - 1;
+                mz = S->lat[2] - 1;
+                x = (uint32_t)(local / ((uint64_t)my * mz));
+                y = (uint32_t)((local / mz) % my);
+                z = (uint32_t)(local % mz);
+                sz = S->lat[2];
+                plane = (uint64_t)S->lat[1] * sz;
+                row = S->lat_base + (uint64_t)x * plane + (uint64_t)y * sz;
+                iso = S->iso;
+                have = false;
+            }
+            const uint64_t r00 = row + z, r10 = r00 + plane, r01 = r00 + sz, r11 = r10 + sz;
+            auto below = [&](uint64_t idx, int bit) { return __ldg(&lattice[idx].x) < iso ? 1u << bit : 0u; };
+            uint32_t ci = have ? prev >> 4 : below(r00, 0) | below(r10, 1) | below(r11, 2) | below(r01, 3);
+            ci |= below(r00 + 1, 4) | below(r10 + 1, 5) | below(r11 + 1, 6) | below(r01 + 1, 7);
+            prev = ci;
+            cases[i] = (uint8_t)ci;
+            v[k] = g_mc_edge_mask[ci] ? (uint32_t)(g_mc_num_verts[ci] / 3) : 0u;
+            have = true;
+            if (++z == mz) {
+                z = 0;
+                have = false;
+                row += sz;
+                if (++y == my) {
+                    y = 0;
+                    ++x;
+                    row = S->lat_base + (uint64_t)x * plane;
+                }
+            }
         }
-        cases[i] = (uint8_t)ci;
-        return g_mc_edge_mask[ci] ? (uint32_t)(g_mc_num_verts[ci] / 3) : 0u;
     }
 };
 
@@ -237,86 +267,137 @@ __device__ __forceinline__ int snap_select(float iso, float v1, float v2, float 
     return 0;
 }
 
-__global__ void __launch_bounds__(256)
+// Corner c of a cube as (x, y, z) offsets and edge e as its two corners, in the
+// reference's numbering (surface.hpp): constant expressions, so that unrolled loops
+// index the corner registers directly.
+__host__ __device__ constexpr uint32_t corner_x(int c) { return ((c + 1) >> 1) & 1; }
+__host__ __device__ constexpr uint32_t corner_y(int c) { return (c >> 1) & 1; }
+__host__ __device__ constexpr uint32_t corner_z(int c) { return c >> 2; }
+__host__ __device__ constexpr int edge_a(int e) { return e < 8 ? e : e - 8; }
+__host__ __device__ constexpr int edge_b(int e) { return e < 8 ? ((e & 4) | ((e + 1) & 3)) : e - 4; }
+
+constexpr int kEmitWarps = 4, kEmitCubesPerLane = 4;
+constexpr int kEmitCubes = kEmitWarps * 32 * kEmitCubesPerLane;  // cubes per CTA
+constexpr int kEdgeWords = 12 * 7 + 1;  // per lane: 12 edge vertices (position, normal, colour), padded
+
+// Triangles of the cubes [i0, i0 + kEmitCubes) at their scanned offsets.  Each warp
+// takes 128 cubes, lists those that have triangles (in cube order), and handles them 32
+// at a time: a lane computes one cube's edge vertices into shared memory, then the
+// warp writes the group's triangles -- contiguous in the output, since the offsets are
+// an exclusive scan in cube order -- word by word, 32 consecutive words per store.
+__global__ void __launch_bounds__(kEmitWarps * 32)
     k_emit(const SceneDev *__restrict__ scenes, uint32_t scene_begin, uint32_t scene_end,
            const float4 *__restrict__ lattice, const uint32_t *__restrict__ lattice_col,
            const uint8_t *__restrict__ cases, const uint32_t *__restrict__ offsets, uint64_t cube_begin,
            uint64_t cubes, fgb_mesh_triangle *__restrict__ out, uint64_t cap, float snap, uint32_t *err) {
-    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cubes) return;
-    const uint32_t ci = cases[i];
-    if (!g_mc_edge_mask[ci]) return;
-    const uint32_t nv = g_mc_num_verts[ci];
-    const uint64_t o0 = offsets[i];
-    if (o0 + nv / 3 > cap) {
-        raise_error(err, ERR_MESH_CAPACITY);
-        return;
-    }
-    const uint64_t q = cube_begin + i;
-    const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
-    const SceneDev &S = scenes[s];
-    const uint64_t local = q - S.cube_base;
-    const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
-    const uint64_t x = local / (my * mz), y = (local / mz) % my, z = local % mz;
-    const uint64_t sy = S.lat[1], sz = S.lat[2];
-    const float iso = S.iso;
-    float val[8], pw[8][3], nrm[8][3];
-    uint32_t col[8];
+    __shared__ float s_edge[kEmitWarps][32][kEdgeWords];
+    __shared__ uint8_t s_act[kEmitWarps][32 * kEmitCubesPerLane];
+    __shared__ uint8_t s_owner[kEmitWarps][32 * 5], s_which[kEmitWarps][32 * 5];
+    __shared__ uint8_t s_case[kEmitWarps][32];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint64_t i0 = (uint64_t)blockIdx.x * kEmitCubes + (uint64_t)w * 32 * kEmitCubesPerLane;
+    // this warp's cubes that have triangles, in cube order
+    uint32_t n_act = 0;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const uint64_t ox = x + c_corner[c][0], oy = y + c_corner[c][1], oz = z + c_corner[c][2];
-        const uint64_t idx = S.lat_base + (ox * sy + oy) * sz + oz;
-        const float4 L = lattice[idx];
-        val[c] = L.x;
-        nrm[c][0] = L.y;
-        nrm[c][1] = L.z;
-        nrm[c][2] = L.w;
-        col[c] = lattice_col[idx];
-        pw[c][0] = ((float)ox * S.lat_step + S.lat_origin[0]) * S.scale;
-        pw[c][1] = ((float)oy * S.lat_step + S.lat_origin[1]) * S.scale;
-        pw[c][2] = ((float)oz * S.lat_step + S.lat_origin[2]) * S.scale;
+    for (int k = 0; k < kEmitCubesPerLane; ++k) {
+        const uint64_t i = i0 + 32u * k + lane;
+        const bool on = i < cubes && g_mc_edge_mask[cases[i]] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, on);
+        if (on) s_act[w][n_act + __popc(m & lanemask_lt())] = (uint8_t)(32u * k + lane);
+        n_act += __popc(m);
     }
-    const uint16_t em = g_mc_edge_mask[ci];
-    float ev[12][3], en[12][3];
-    uint32_t ec[12];
+    __syncwarp();
+    float *ed = s_edge[w][lane];
+    for (uint32_t g = 0; g < n_act; g += 32) {
+        const bool mine = g + lane < n_act;
+        const uint64_t i = i0 + (mine ? s_act[w][g + lane] : s_act[w][g]);
+        const uint32_t ci = cases[i];
+        const uint32_t ntri = mine ? g_mc_num_verts[ci] / 3 : 0u;
+        // the group's triangles start at the offset of its first cube
+        uint32_t incl = ntri;
 #pragma unroll
-    for (int e = 0; e < 12; ++e) {
-        if (!(em & (1u << e))) continue;
-        const int a = c_edge[e][0], b = c_edge[e][1];
-        const int sel = snap_select(iso, val[a], val[b], snap);
-        if (sel) {
-            const int k = sel == 1 ? a : b;
-            for (int d = 0; d < 3; ++d) {
-                ev[e][d] = pw[k][d];
-                en[e][d] = nrm[k][d];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t tri_total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint64_t t0 = offsets[i0 + s_act[w][g]];
+        if (mine) {
+            s_case[w][lane] = (uint8_t)ci;
+            for (uint32_t t = 0; t < ntri; ++t) {
+                s_owner[w][incl - ntri + t] = (uint8_t)lane;
+                s_which[w][incl - ntri + t] = (uint8_t)t;
             }
-            ec[e] = col[k];
+            const uint64_t q = cube_begin + i;
+            const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
+            const SceneDev &S = scenes[s];
+            const uint64_t local = q - S.cube_base;
+            const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
+            const uint32_t x = (uint32_t)(local / (my * mz)), y = (uint32_t)((local / mz) % my),
+                           z = (uint32_t)(local % mz);
+            const uint64_t sy = S.lat[1], sz = S.lat[2];
+            const float iso = S.iso;
+            float val[8], pw[8][3], nrm[8][3];
+            uint32_t col[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const uint32_t ox = x + corner_x(c), oy = y + corner_y(c), oz = z + corner_z(c);
+                const uint64_t idx = S.lat_base + ((uint64_t)ox * sy + oy) * sz + oz;
+                const float4 L = __ldg(&lattice[idx]);
+                val[c] = L.x;
+                nrm[c][0] = L.y;
+                nrm[c][1] = L.z;
+                nrm[c][2] = L.w;
+                col[c] = __ldg(&lattice_col[idx]);
+                pw[c][0] = ((float)ox * S.lat_step + S.lat_origin[0]) * S.scale;
+                pw[c][1] = ((float)oy * S.lat_step + S.lat_origin[1]) * S.scale;
+                pw[c][2] = ((float)oz * S.lat_step + S.lat_origin[2]) * S.scale;
+            }
+            const uint16_t em = g_mc_edge_mask[ci];
+#pragma unroll
+            for (int e = 0; e < 12; ++e) {
+                if (!(em & (1u << e))) continue;
+                const int a = edge_a(e), b = edge_b(e);
+                float *o = ed + 7 * e;
+                const int sel = snap_select(iso, val[a], val[b], snap);
+                if (sel) {
+                    const bool first = sel == 1;
+                    for (int d = 0; d < 3; ++d) {
+                        o[d] = first ? pw[a][d] : pw[b][d];
+                        o[3 + d] = first ? nrm[a][d] : nrm[b][d];
+                    }
+                    o[6] = __uint_as_float(first ? col[a] : col[b]);
+                } else {
+                    const float mu = (iso - val[a]) / (val[b] - val[a]);
+                    for (int d = 0; d < 3; ++d) {
+                        o[d] = pw[a][d] + (pw[b][d] - pw[a][d]) * mu;
+                        o[3 + d] = nrm[a][d] + (nrm[b][d] - nrm[a][d]) * mu;
+                    }
+                    float ch[4];
+                    for (int c = 0; c < 4; ++c) {
+                        const float fa = (float)argb_channel(col[a], c), fb = (float)argb_channel(col[b], c);
+                        ch[c] = fa + (fb - fa) * mu;
+                    }
+                    o[6] = __uint_as_float(argb_pack(ch));
+                }
+            }
+        }
+        __syncwarp();
+        // the group's triangles, 21 words each, written in order
+        if (t0 + tri_total > cap) {
+            if (lane == 0) raise_error(err, ERR_MESH_CAPACITY);
         } else {
-            const float mu = (iso - val[a]) / (val[b] - val[a]);
-            for (int d = 0; d < 3; ++d) {
-                ev[e][d] = pw[a][d] + (pw[b][d] - pw[a][d]) * mu;
-                en[e][d] = nrm[a][d] + (nrm[b][d] - nrm[a][d]) * mu;
+            uint32_t *dst = reinterpret_cast<uint32_t *>(out + t0);
+            for (uint32_t wd = lane; wd < 21u * tri_total; wd += 32) {
+                const uint32_t t = wd / 21u, f = wd - 21u * t;
+                const uint32_t owner = s_owner[w][t], tt = s_which[w][t];
+                const uint32_t vert = f < 18u ? (f < 9u ? f / 3u : (f - 9u) / 3u) : f - 18u;
+                const uint32_t e = g_mc_tri[s_case[w][owner]][3u * tt + vert];
+                const uint32_t comp = f < 9u ? f % 3u : f < 18u ? 3u + (f - 9u) % 3u : 6u;
+                dst[wd] = __float_as_uint(s_edge[w][owner][7u * e + comp]);
             }
-            float ch[4];
-            for (int c = 0; c < 4; ++c) {
-                const float fa = (float)argb_channel(col[a], c), fb = (float)argb_channel(col[b], c);
-                ch[c] = fa + (fb - fa) * mu;
-            }
-            ec[e] = argb_pack(ch);
         }
-    }
-    for (uint32_t t = 0; t < nv; t += 3) {
-        fgb_mesh_triangle *m = &out[o0 + t / 3];
-        for (int j = 0; j < 3; ++j) {
-            const int e = g_mc_tri[ci][t + j];
-            m->v[3 * j] = ev[e][0];
-            m->v[3 * j + 1] = ev[e][1];
-            m->v[3 * j + 2] = ev[e][2];
-            m->n[3 * j] = en[e][0];
-            m->n[3 * j + 1] = en[e][1];
-            m->n[3 * j + 2] = en[e][2];
-            m->c[j] = ec[e];
-        }
+        __syncwarp();
     }
 }
 
@@ -353,7 +434,7 @@ cudaError_t launch_surface_emit(const SurfaceView &v, fgb_mesh_triangle *out, ui
                                 uint64_t *launches) {
     const uint64_t cubes = v.cube_end - v.cube_begin;
     if (!cubes || !cap) return cudaSuccess;
-    k_emit<<<(unsigned)((cubes + 255) / 256), 256, 0, st>>>(v.scenes, v.scene_begin, v.scene_end, v.lattice,
+    k_emit<<<(unsigned)((cubes + kEmitCubes - 1) / kEmitCubes), kEmitWarps * 32, 0, st>>>(v.scenes, v.scene_begin, v.scene_end, v.lattice,
                                                            v.lattice_col, v.cases, v.offsets, v.cube_begin, cubes,
                                                            out, cap, snap_threshold(), v.err);
     if (launches) *launches += 1;

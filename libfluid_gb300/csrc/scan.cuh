@@ -5,11 +5,14 @@
 // include/fluid/oclsph.hpp:450-465): here the counts become exclusive offsets on the
 // device in one pass, so triangles can be written at fixed, deterministic positions.
 //
-// The input is produced by a loader functor (`uint32_t operator()(uint64_t i)`), so
+// The input is produced by a loader functor (`uint32_t operator()(uint64_t i)`, or a
+// `run` over a thread's consecutive items), so
 // the marching-cubes case classification is fused into the scan's load.
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "fgb_device.cuh"
@@ -22,6 +25,14 @@ LookbackCtl lookback_ctl();
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
+
+// A loader may also offer `run(first, n, v)`, filling v[0..kScanItems) with the items
+// first, first + 1, ... (0 at and past n) in one call, when consecutive items share work.
+template <class L, class = void>
+struct kLoadsRuns : std::false_type {};
+template <class L>
+struct kLoadsRuns<L, std::void_t<decltype(std::declval<const L &>().run(
+                         uint64_t{}, uint64_t{}, std::declval<uint32_t (&)[kScanItems]>()))>> : std::true_type {};
 
 constexpr unsigned long long kScanAggregate = 1ull << 32;
 constexpr unsigned long long kScanInclusive = 2ull << 32;
@@ -41,12 +52,17 @@ __global__ void __launch_bounds__(kScanThreads)
 
     uint32_t v[kScanItems];
     uint32_t sum = 0;
+    if constexpr (kLoadsRuns<Load>::value) {
+        load.run(first, n, v);
+    } else {
 #pragma unroll
-    for (int i = 0; i < kScanItems; ++i) {
-        uint64_t idx = first + i;
-        v[i] = idx < n ? load(idx) : 0u;
-        sum += v[i];
+        for (int i = 0; i < kScanItems; ++i) {
+            uint64_t idx = first + i;
+            v[i] = idx < n ? load(idx) : 0u;
+        }
     }
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) sum += v[i];
     uint32_t x = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
