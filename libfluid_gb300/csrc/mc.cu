@@ -152,10 +152,10 @@ __global__ void __launch_bounds__(256)
     const uint64_t brick = brick_begin + blockIdx.x;
     const uint32_t s = find_scene<Base::kBrick>(scenes, scene_begin, scene_end, brick);
     const SceneDev &S = scenes[s];
-    const uint64_t local = brick - S.brick_base;
-    const uint64_t nby = (S.lat[1] + kBrickY - 1) / kBrickY, nbz = (S.lat[2] + kBrickZ - 1) / kBrickZ;
-    const uint32_t bz = (uint32_t)(local % nbz), by = (uint32_t)((local / nbz) % nby),
-                   bx = (uint32_t)(local / (nbz * nby));
+    // 32-bit index arithmetic: a scene's bricks and cubes number below 2^32
+    const uint32_t local = (uint32_t)(brick - S.brick_base);
+    const uint32_t nby = (S.lat[1] + kBrickY - 1) / kBrickY, nbz = (S.lat[2] + kBrickZ - 1) / kBrickZ;
+    const uint32_t bz = local % nbz, by = (local / nbz) % nby, bx = local / (nbz * nby);
     const uint32_t w = threadIdx.x >> 5, l = threadIdx.x & 31u;
     const uint32_t ix = bx * kBrickX + (w & 1u) * 2u + (l & 1u);
     const uint32_t iy = by * kBrickY + ((w >> 1) & 1u) * 4u + ((l >> 1) & 3u);
@@ -222,13 +222,13 @@ struct CubeCount {
             if (!S || x >= mx) {  // first cube, or past the end of a scene's cubes
                 const uint64_t q = cube_begin + i;
                 S = &scenes[find_scene<Base::kCube>(scenes, scene_begin, scene_end, q)];
-                const uint64_t local = q - S->cube_base;
+                const uint32_t local = (uint32_t)(q - S->cube_base);
                 mx = S->lat[0] - 1;
                 my = S->lat[1] - 1;
                 mz = S->lat[2] - 1;
-                x = (uint32_t)(local / ((uint64_t)my * mz));
-                y = (uint32_t)((local / mz) % my);
-                z = (uint32_t)(local % mz);
+                x = local / (my * mz);
+                y = (local / mz) % my;
+                z = local % mz;
                 sz = S->lat[2];
                 plane = (uint64_t)S->lat[1] * sz;
                 row = S->lat_base + (uint64_t)x * plane + (uint64_t)y * sz;
@@ -331,10 +331,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32)
             const uint64_t q = cube_begin + i;
             const uint32_t s = find_scene<Base::kCube>(scenes, scene_begin, scene_end, q);
             const SceneDev &S = scenes[s];
-            const uint64_t local = q - S.cube_base;
-            const uint64_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
-            const uint32_t x = (uint32_t)(local / (my * mz)), y = (uint32_t)((local / mz) % my),
-                           z = (uint32_t)(local % mz);
+            const uint32_t local = (uint32_t)(q - S.cube_base);
+            const uint32_t my = S.lat[1] - 1, mz = S.lat[2] - 1;
+            const uint32_t x = local / (my * mz), y = (local / mz) % my, z = local % mz;
             const uint64_t sy = S.lat[1], sz = S.lat[2];
             const float iso = S.iso;
             float val[8], pw[8][3], nrm[8][3];

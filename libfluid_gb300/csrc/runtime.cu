@@ -1235,6 +1235,7 @@ static int batch_init(fgb_batch *b) {
     b->cube_total = cubes;
     b->brick_total = bricks;
     if (cubes > 0xffffffffull) return fail(FGB_ERR_CAPACITY, "batch: more than 2^32-1 marching cubes");
+    if (bricks > 0x7fffffffull) return fail(FGB_ERR_CAPACITY, "batch: more than 2^31-1 lattice bricks");
     b->mbits = 3 * bits_for(max_ext);
     b->sbits = bits_for(b->n_scenes - 1);
     b->key_bits = b->mbits + b->sbits;
