@@ -141,6 +141,31 @@ __device__ __forceinline__ void field_sums(const SceneDev &S, const Phys &ph, co
     acc[3] = nz;
 }
 
+// Whether any cell within one cell of the warp's nodes' cells holds a particle.  The
+// nodes of a warp lie in a few adjacent cells, so the lanes share the table lookups of
+// that common neighbourhood (at most 128 cells; larger ones are not checked).  When
+// every cell is empty, every node's walk finds no candidate and its sums stay zero.
+__device__ __forceinline__ bool warp_cells_occupied(const SceneDev &S, const uint2 *__restrict__ cells,
+                                                    unsigned act, const int *cc) {
+    uint32_t lo[3], n[3];
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t mn = __reduce_min_sync(act, (uint32_t)cc[a]), mx = __reduce_max_sync(act, (uint32_t)cc[a]);
+        lo[a] = mn > 0 ? mn - 1 : 0;
+        n[a] = (mx < S.ext[a] ? mx + 1 : S.ext[a]) - lo[a] + 1;
+    }
+    const uint32_t total = n[0] * n[1] * n[2];
+    if (total > 128u) return true;
+    const uint2 *tbl = cells + S.table_base;
+    const uint32_t r = __popc(act & lanemask_lt()), cnt = __popc(act);
+    bool any = false;
+    for (uint32_t k = r; k < total; k += cnt) {
+        const uint32_t x = lo[0] + k % n[0], y = lo[1] + (k / n[0]) % n[1], z = lo[2] + k / (n[0] * n[1]);
+        const uint2 c = __ldg(&tbl[spread10(x) | (spread10(y) << 1) | (spread10(z) << 2)]);
+        any |= c.x < c.y;
+    }
+    return __any_sync(act, any);
+}
+
 // One CTA per brick of kBrickX x kBrickY x kBrickZ lattice nodes of one scene; every
 // node's value is its own walk's, whatever the thread that computes it.
 template <int PROFILE>
@@ -160,26 +185,32 @@ __global__ void __launch_bounds__(256)
     const uint32_t ix = bx * kBrickX + (w & 1u) * 2u + (l & 1u);
     const uint32_t iy = by * kBrickY + ((w >> 1) & 1u) * 4u + ((l >> 1) & 3u);
     const uint32_t iz = bz * kBrickZ + (w >> 2) * 4u + (l >> 3);
-    if (ix >= S.lat[0] || iy >= S.lat[1] || iz >= S.lat[2]) return;
-    const uint64_t q = S.lat_base + ((uint64_t)ix * S.lat[1] + iy) * S.lat[2] + iz;
+    const bool valid = ix < S.lat[0] && iy < S.lat[1] && iz < S.lat[2];
     const float node[3] = {S.lat_origin[0] + (float)ix * S.lat_step, S.lat_origin[1] + (float)iy * S.lat_step,
                            S.lat_origin[2] + (float)iz * S.lat_step};
-    int cc[3];
-    if (PROFILE == FGB_PROFILE_REF) {
-        const uint32_t id[3] = {ix, iy, iz};
-        for (int a = 0; a < 3; ++a) {
-            uint32_t c = (uint32_t)((float)id[a] / S.resolution);
-            cc[a] = (int)(c > S.ext[a] ? S.ext[a] : c);
+    int cc[3] = {0, 0, 0};
+    if (valid) {
+        if (PROFILE == FGB_PROFILE_REF) {
+            const uint32_t id[3] = {ix, iy, iz};
+            for (int a = 0; a < 3; ++a) {
+                uint32_t c = (uint32_t)((float)id[a] / S.resolution);
+                cc[a] = (int)(c > S.ext[a] ? S.ext[a] : c);
+            }
+        } else {
+            for (int a = 0; a < 3; ++a) cc[a] = (int)quantise(node[a], S.min_ext[a], ph.h, S.ext[a]);
         }
-    } else {
-        for (int a = 0; a < 3; ++a) cc[a] = (int)quantise(node[a], S.min_ext[a], ph.h, S.ext[a]);
     }
-    float acc[4];
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    if (!valid) return;
+    const uint64_t q = S.lat_base + ((uint64_t)ix * S.lat[1] + iy) * S.lat[2] + iz;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
     // channel sums as integers: below 2^24, so equal to the float sums in any order
     uint32_t cl[4] = {0, 0, 0, 0};
     uint32_t N = 0;
-    if (S.scale == 1.f) field_sums<PROFILE, true>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
-    else field_sums<PROFILE, false>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
+    if (warp_cells_occupied(S, cells, act, cc)) {
+        if (S.scale == 1.f) field_sums<PROFILE, true>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
+        else field_sums<PROFILE, false>(S, ph, cells, xs, type, col, cc, node, acc, cl, N);
+    }
     float v = acc[0], nx = acc[1], ny = acc[2], nz = acc[3];
     if (PROFILE != FGB_PROFILE_REF) v = v * ph.poly6f;
     const float nl = sqrtf(nx * nx + ny * ny + nz * nz);
