@@ -279,6 +279,36 @@ def test_surface_with_obstacles_and_colours_on_identical_input(oracle_mod):
     solver.close()
 
 
+@pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
+def test_surface_with_a_world_scale_on_identical_input(oracle_mod, profile):
+    # world units twice the solver's: the field divides each position by the scale
+    # (baseline) or scales the node (ref), and the range tests see those values
+    params = capi.params(profile, H)
+    parts, cfg = scenes.dam_break((14, 12, 14), (1.6, 1.6, 1.6), seed=47)
+    cfg.scale = 2.0
+    for a in range(3):
+        cfg.min_bound[a] *= 2.0
+        cfg.max_bound[a] *= 2.0
+    parts["position"] *= np.float32(2.0)
+    if profile == capi.PROFILE_REF:
+        cfg.isolevel = 100.0
+    ref = scenes.copy_particles(parts)
+    solver = SphSolver(params=params)
+    batch = Batch(solver, [(parts, cfg)])
+    tris = batch.surface(0)
+    otris, olat, ocol, ocases = oracle_mod.surface(params, cfg, ref, want_lattice=True)
+    lat = batch.probe(capi.PROBE_LATTICE, np.float32).reshape(-1, 4)
+    cases = batch.probe(capi.PROBE_CUBE_CASES, np.uint8)
+    assert batch.error_flags() == 0
+    assert np.abs(lat[:, 0] - olat[:, 0]).max() <= 1e-5 * max(params.rho0, np.abs(olat[:, 0]).max())
+    assert (cases == ocases).all()
+    assert len(tris) == len(otris) > 0
+    assert np.abs(tris[:, :9] - otris[:, :9]).max() <= 2.0 * VERT_TOL
+    assert (tris[:, 18:].view(np.uint32) == otris[:, 18:].view(np.uint32)).all()
+    batch.close()
+    solver.close()
+
+
 def test_advance_drop_in_matches_oracle(oracle_mod):
     params = capi.params(capi.PROFILE_BASELINE, H)
     parts, cfg = scenes.dam_break((20, 20, 20), (2.0, 2.0, 2.0), seed=51)
