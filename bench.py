@@ -281,7 +281,7 @@ def bench_batched(params, steps=100, mc_every=10, tune=True, rank=0, world=1):
                 b.step(1)
             if s % mc_every == 0:
                 for b in singles:
-                    b.surface(0)
+                    b.surface_all()  # triangles left on the device, as in the batched arm
         for b in singles:
             b.sync()
         t_loop = time.perf_counter() - t0
