@@ -377,7 +377,8 @@ def bench_large(params, steps=20, warmup=3, tune=True):
             "hbm_peak_kind": peak_kind, "step_hbm_frac": gbs / peak, "error_flags": flags, "surface": surface,
             "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
                            "persistent": bool(tuned.persistent),
-                           "particles_per_thread": int(tuned.particles_per_thread)} if tuned else None)}
+                           "particles_per_thread": int(tuned.particles_per_thread),
+                           "verlet_lists": bool(tuned.verlet)} if tuned else None)}
 
 
 def bench_ref_profile(steps=30, warmup=5, tune=True):
@@ -785,6 +786,7 @@ def run_ours(args):
                       "autotuned": ({"block": int(tuned.block), "skin_h": round(float(tuned.skin), 3),
                                      "persistent": bool(tuned.persistent),
                                      "particles_per_thread": int(tuned.particles_per_thread),
+                                     "verlet_lists": bool(tuned.verlet),
                                      "trial_steps": int(tuned.steps)} if tuned else None)},
             # direct: kernels read id/type/mass/colour/position/velocity (44 B) from the
             # caller's arrays and write them back; staged: pinned float4 x, float4 v,

@@ -247,7 +247,9 @@ uint64_t fgb_batch_launch_count(const fgb_batch *b);
 int fgb_batch_set_timing(fgb_batch *b, int on);
 /* Autotuner: runs the batch's next steps under each candidate launch shape (gather
  * CTA size 64, 128, 256 at the current Verlet skin, then skins 0.1-0.3 h at the best
- * size; steps_per_trial steps each, the first untimed), keeps the fastest, and caches
+ * size, then persistent tile queues of 1 and 2 particles per thread, then near rows
+ * with and without Verlet lists in turn (five trials); steps_per_trial steps each, the
+ * first untimed), keeps the fastest, and caches
  * it in the solver for every later batch of the same physics profile and size
  * bucket (floor(log2(particles))).  The trial steps are ordinary steps: no knob
  * changes a result, so a tuned batch computes the same bits as an untuned one.
@@ -260,6 +262,7 @@ typedef struct fgb_tune_result {
     uint32_t trials, steps;
     uint32_t persistent; /* 1: the gathers run as persistent grids over a tile queue */
     uint32_t particles_per_thread;  /* of a persistent grid's tiles (1 otherwise) */
+    uint32_t verlet;     /* 1: steps build Verlet lists beside the near rows; 0: near rows only */
 } fgb_tune_result;
 int fgb_batch_autotune(fgb_batch *b, uint32_t steps_per_trial, fgb_tune_result *out);
 int fgb_batch_stage_times(fgb_batch *b, float *ms, uint32_t max, uint32_t *count);

@@ -232,7 +232,7 @@ def from_records(rec):
 class TuneResult(ctypes.Structure):
     _fields_ = [("block", ctypes.c_uint32), ("skin", ctypes.c_float), ("ms_per_step", ctypes.c_float),
                 ("trials", ctypes.c_uint32), ("steps", ctypes.c_uint32), ("persistent", ctypes.c_uint32),
-                ("particles_per_thread", ctypes.c_uint32)]
+                ("particles_per_thread", ctypes.c_uint32), ("verlet", ctypes.c_uint32)]
 
 
 P = ctypes.POINTER

@@ -71,6 +71,7 @@ struct StepView {
     // of the step (slots_of_step), ppt particles per thread of a tile
     uint32_t *queue;
     uint32_t ppt;
+    uint32_t verlet_off;  // build near rows but no Verlet lists
     // {1 while steps build Verlet lists, movers of the step} (null: lists every step)
     uint32_t *list_policy;
     uint32_t list_min_use;  // percent of a pass's particles that keeps lists on
@@ -111,6 +112,12 @@ struct StepView {
 
 
 constexpr uint16_t kListOverflow = 0xffffu;
+// k_list_policy's words per scene: [0] 1 while steps build the scene's Verlet lists and
+// near rows; counts of the current step: [1] fluid particles that its last delta pass
+// moved more than half the skin, [2] all fluid particles of that pass, [3] particles of
+// its second lambda pass that ran on a near row or a list that held, [4] those that
+// walked; [5] steps since the lists were turned off.
+constexpr uint32_t kPolicyWords = 6;
 
 void launch_fill_u32(uint32_t *p, uint64_t n, uint32_t value, cudaStream_t st);
 void launch_iota_u32(uint32_t *p, uint64_t n, cudaStream_t st);  // p[i] = i

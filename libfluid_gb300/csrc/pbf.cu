@@ -196,6 +196,7 @@ struct GatherArgs {
     // null: one particle per thread over a flat grid; else this launch's tile counter
     // (zero at launch) for a persistent grid taking tiles of ppt x blockDim particles
     uint32_t *queue;
+    uint32_t verlet_off;
     uint32_t ppt;
     // null, or per scene: kPolicyWords words of k_list_policy's state
     uint32_t *list_policy;
@@ -458,12 +459,6 @@ __device__ __forceinline__ void close_hits_empty(const GatherArgs &A, uint32_t a
     if (A.hcap) A.hcount[a] = 0;
 }
 
-// k_list_policy's words per scene: [0] 1 while steps build the scene's Verlet lists and
-// near rows; counts of the current step: [1] fluid particles that its last delta pass
-// moved more than half the skin, [2] all fluid particles of that pass, [3] particles of
-// its second lambda pass that ran on a near row or a list that held, [4] those that
-// walked; [5] steps since the lists were turned off.
-constexpr uint32_t kPolicyWords = 6;
 
 // The list policy's sample: per scene of the warp, the particles whose list (or near
 // row) served this pass and those that walked.
@@ -533,7 +528,7 @@ __device__ __forceinline__ bool lists_on(const GatherArgs &A, uint32_t sc) {
 template <class Sp>
 __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, const Sp &sp, const float4 *__restrict__ ps) {
     if (a >= A.n) return;
-    if (!lists_on(A, scene_of(A.keys[a], A.mbits))) {  // no lists this step: every pass walks
+    if (A.verlet_off || !lists_on(A, scene_of(A.keys[a], A.mbits))) {  // no lists this step: every pass walks
         A.ncount[a] = kListOverflow;
         return;
     }
@@ -1348,6 +1343,7 @@ GatherArgs gather_args(const StepView &s) {
     A.list_policy = s.cap ? s.list_policy : nullptr;
     A.count_lists = 0;  // the second lambda pass's launch sets it
     A.ppt = s.ppt ? s.ppt : 1;
+    A.verlet_off = s.verlet_off;
     A.mass_range = s.mass_range;
     return A;
 }

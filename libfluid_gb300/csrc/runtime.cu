@@ -476,6 +476,7 @@ struct fgb_solver {
         float skin;
         bool persistent;
         uint32_t ppt;
+        bool verlet_off;
     };
     std::map<uint32_t, Tuned> tuned;
     // row capacities (Verlet, hit) that batches grew to, per (profile, log2 n) bucket:
@@ -554,6 +555,7 @@ struct fgb_batch {
     Dev<uint16_t> hcount;
     uint32_t hit_cap = 64;
     uint32_t list_cap = 96;
+    uint32_t verlet_off = 0;
     float skin_frac = 0.2f;
     // persistent gathers: CTAs take tiles of ppt x block particles from per-launch
     // counters (queue, zeroed at the start of every step) instead of a flat grid
@@ -667,6 +669,7 @@ struct fgb_batch {
         s.list_policy = list_policy.p;
         s.list_min_use = list_min_use;
         s.ppt = persistent ? ppt : 1;
+        s.verlet_off = verlet_off;
         s.iterations = iterations;
         s.sm_count = sm_count;
         s.nlist = nlist.p;
@@ -784,11 +787,22 @@ struct fgb_batch {
         FGB_CUDA(cudaEventCreate(&e0), "autotune event");
         FGB_CUDA(cudaEventCreate(&e1), "autotune event");
         uint32_t trials = 0, steps = 0;
-        auto trial = [&](int blk, float skin, bool pers, uint32_t per_thread, float *ms) -> int {
+        auto trial = [&](int blk, float skin, bool pers, uint32_t per_thread, float *ms, bool voff = false) -> int {
             block = blk;
             skin_frac = skin;
             persistent = pers;
             ppt = per_thread;
+            verlet_off = voff ? 1u : 0u;
+            // every trial starts from the list policy of a fresh batch (lists on), so
+            // that one trial's choices do not carry into the next
+            if (list_policy.p) {
+                std::vector<uint32_t> init(kPolicyWords * (size_t)n_scenes, 0u);
+                for (uint32_t k = 0; k < n_scenes; ++k) init[kPolicyWords * k] = 1u;
+                if (cudaMemcpyAsync(list_policy.p, init.data(), init.size() * sizeof(uint32_t),
+                                    cudaMemcpyHostToDevice, stream()) != cudaSuccess ||
+                    cudaStreamSynchronize(stream()) != cudaSuccess)
+                    return fail(FGB_ERR_CUDA, "autotune: list policy");
+            }
             for (auto &g : graph)
                 if (g) cudaGraphExecDestroy(g), g = nullptr;
             graphs_ok = false;
@@ -827,22 +841,37 @@ struct fgb_batch {
             rc = trial(best_block, best_skin, true, per_thread, &ms);
             if (!rc && ms < best_ms) best_ms = ms, best_pers = true, best_ppt = per_thread;
         }
+        // near rows without Verlet lists: trials alternate with and without them (with,
+        // without, with, without, with), so a drift of the flow that is linear over the
+        // five trials weighs both equally
+        bool best_voff = false;
+        if (!rc && list_cap && hit_cap) {
+            float on = 0.f, off = 0.f, t = 0.f;
+            for (int k = 0; k < 5 && !rc; ++k) {
+                rc = trial(best_block, best_skin, best_pers, best_ppt, &t, k & 1);
+                if (k & 1) off += t / 2.f;
+                else on += t / 3.f;
+            }
+            if (!rc && off < 0.995f * on) best_voff = true, best_ms = off;
+        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         block = best_block;
         skin_frac = best_skin;
         persistent = best_pers;
         ppt = best_ppt;
+        verlet_off = best_voff ? 1u : 0u;
         for (auto &g : graph)
             if (g) cudaGraphExecDestroy(g), g = nullptr;
         graphs_ok = false;
         if (rc) return rc;
-        solver->tuned[tune_bucket(solver->params.profile, n)] = {best_block, best_skin, best_pers, best_ppt};
+        solver->tuned[tune_bucket(solver->params.profile, n)] = {best_block, best_skin, best_pers, best_ppt, best_voff};
         if (out) {
             out->block = (uint32_t)best_block;
             out->skin = best_skin;
             out->persistent = best_pers ? 1u : 0u;
             out->particles_per_thread = best_ppt;
+            out->verlet = best_voff ? 0u : 1u;
             out->ms_per_step = best_ms;
             out->trials = trials;
             out->steps = steps;
@@ -1268,18 +1297,20 @@ static int batch_init(fgb_batch *b) {
             b->skin_frac = it->second.skin;
             b->persistent = it->second.persistent;
             b->ppt = it->second.ppt;
+            b->verlet_off = it->second.verlet_off ? 1u : 0u;
         }
     }
     if (const char *e = getenv("FGB_LIST_SKIN")) b->skin_frac = (float)atof(e);
+    if (const char *e = getenv("FGB_VERLET")) b->verlet_off = atoi(e) == 0;
     if (const char *e = getenv("FGB_PERSISTENT")) b->persistent = atoi(e) != 0;
     if (const char *e = getenv("FGB_PPT")) b->ppt = (uint32_t)std::max(1, std::min(8, atoi(e)));
     cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, s->device);
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
-        FGB_CUDA(b->list_policy.alloc(6 * (uint64_t)b->n_scenes), "batch alloc");
+        FGB_CUDA(b->list_policy.alloc(kPolicyWords * (uint64_t)b->n_scenes), "batch alloc");
         if (const char *e = getenv("FGB_LIST_MIN_USE")) b->list_min_use = (uint32_t)std::max(0, std::min(101, atoi(e)));
-        std::vector<uint32_t> init(6 * (size_t)b->n_scenes, 0u);
-        for (uint32_t k = 0; k < b->n_scenes; ++k) init[6 * k] = 1u;  // the first step builds lists
+        std::vector<uint32_t> init(kPolicyWords * (size_t)b->n_scenes, 0u);
+        for (uint32_t k = 0; k < b->n_scenes; ++k) init[kPolicyWords * k] = 1u;  // the first step builds lists
         FGB_CUDA(cudaMemcpy(b->list_policy.p, init.data(), init.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
                  "batch alloc");
     }

@@ -408,10 +408,11 @@ def test_autotune_changes_no_result():
     tuned_solver, plain_solver = SphSolver(params=params), SphSolver(params=params)
     a = Batch(tuned_solver, [(scenes.copy_particles(parts), cfg)])
     r = a.autotune(2)
-    # three CTA sizes, the four other skins, then persistent tile queues of 1 and 2
-    # particles per thread
-    assert r.block in (64, 128, 256) and r.trials == 9 and r.steps == 18
-    assert r.persistent in (0, 1) and r.particles_per_thread in (1, 2)
+    # three CTA sizes, the four other skins, persistent tile queues of 1 and 2
+    # particles per thread, then near rows with and without Verlet lists in turn
+    # (five trials)
+    assert r.block in (64, 128, 256) and r.trials == 14 and r.steps == 28
+    assert r.persistent in (0, 1) and r.particles_per_thread in (1, 2) and r.verlet in (0, 1)
     assert any(abs(r.skin - s) < 1e-6 for s in (0.1, 0.15, 0.2, 0.25, 0.3))
     b = Batch(plain_solver, [(scenes.copy_particles(parts), cfg)])
     b.step(r.steps)
@@ -424,6 +425,29 @@ def test_autotune_changes_no_result():
         x.close()
     tuned_solver.close()
     plain_solver.close()
+
+
+@pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
+def test_near_rows_without_verlet_lists_give_the_same_bits(profile, monkeypatch):
+    # FGB_VERLET=0: the first lambda pass walks and writes the near rows, later passes
+    # use them or walk, and the vorticity passes walk; every sum is over the same
+    # neighbours in the same order
+    params = capi.params(profile, H)
+    parts, cfg = scenes.dam_break((24, 16, 24), (2.4, 2.4, 2.4), seed=67)
+    parts["type"][::13] = capi.TYPE_OBSTACLE
+    solver = SphSolver(params=params)
+    with_lists = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+    with_lists.step(12)
+    monkeypatch.setenv("FGB_VERLET", "0")
+    near_only = Batch(solver, [(scenes.copy_particles(parts), cfg)])
+    near_only.step(12)
+    a, b = with_lists.download(0), near_only.download(0)
+    for f in ("id", "position", "velocity"):
+        assert (a[f] == b[f]).all(), f
+    assert with_lists.error_flags() == 0 and near_only.error_flags() == 0
+    with_lists.close()
+    near_only.close()
+    solver.close()
 
 
 @pytest.mark.parametrize("profile", [capi.PROFILE_BASELINE, capi.PROFILE_REF])
