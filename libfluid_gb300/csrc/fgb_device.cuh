@@ -164,28 +164,44 @@ __device__ __forceinline__ uint32_t morton_of(uint32_t key, uint32_t mbits) {
     return mbits >= 32 ? key : (key & ((1u << mbits) - 1u));
 }
 
+// The next value of one axis's interleaved bits (mask m) of a Morton code: the bits
+// of the other axes are set so that the carry runs through them, then cleared.
+__device__ __forceinline__ uint32_t morton_inc(uint32_t s, uint32_t m) { return ((s | ~m) + 1u) & m; }
+
+// The cell-table indices (within scene S's table) of the 27 cells around cell
+// (cx, cy, cz), each coordinate in [0, ext], in the reference's order (z, then y, then
+// x ascending: oclsph_kernel.h:155-183), as f(index); cells outside [0, ext] hold no
+// particle and are left out.  The indices advance by Morton increments rather than
+// interleaving every coordinate afresh.
+template <class F>
+__device__ __forceinline__ void for_cell_indices(const SceneDev &S, int cx, int cy, int cz, F &&f) {
+    constexpr uint32_t kMX = 0x09249249u, kMY = kMX << 1, kMZ = kMX << 2;
+    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
+    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
+    const int y0 = cy > 0 ? cy - 1 : 0, y1 = cy < ey ? cy + 1 : ey;
+    const int z0 = cz > 0 ? cz - 1 : 0, z1 = cz < ez ? cz + 1 : ez;
+    const uint32_t sx0 = spread10((uint32_t)x0), sy0 = spread10((uint32_t)y0) << 1;
+    uint32_t sz = spread10((uint32_t)z0) << 2;
+    for (int z = z0; z <= z1; ++z, sz = morton_inc(sz, kMZ)) {
+        uint32_t sy = sy0;
+        for (int y = y0; y <= y1; ++y, sy = morton_inc(sy, kMY)) {
+            const uint32_t yz = sy | sz;
+            uint32_t sx = sx0;
+            for (int x = x0; x <= x1; ++x, sx = morton_inc(sx, kMX)) f(sx | yz);
+        }
+    }
+}
+
 // Visit the particles of the 27 cells around cell (cx, cy, cz) of scene S in the
-// reference's order (dz, dy, dx; x fastest: oclsph_kernel.h:155-183), each cell in
-// sorted order.  Cells outside [0, ext] hold no particle and are skipped.
+// reference's order, each cell in sorted order.
 template <class F>
 __device__ __forceinline__ void for_neighbour_cells(const SceneDev &S, const uint2 *__restrict__ cells, int cx,
                                                     int cy, int cz, F &&f) {
-    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
     const uint2 *tbl = cells + S.table_base;
-    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z > ez) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = cy + dy;
-            if (y < 0 || y > ey) continue;
-            const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-            for (int x = x0; x <= x1; ++x) {
-                const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                for (uint32_t b = c.x; b < c.y; ++b) f(b);
-            }
-        }
-    }
+    for_cell_indices(S, cx, cy, cz, [&](uint32_t k) {
+        const uint2 c = __ldg(&tbl[k]);
+        for (uint32_t b = c.x; b < c.y; ++b) f(b);
+    });
 }
 
 }  // namespace fgb

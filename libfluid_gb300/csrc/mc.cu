@@ -65,31 +65,19 @@ __device__ __forceinline__ uint32_t argb_pack(const float *ch) {
 template <class F>
 __device__ __forceinline__ void field_walk(const SceneDev &S, const uint2 *__restrict__ cells,
                                            const float4 *__restrict__ xs, int cx, int cy, int cz, F &&f) {
-    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
     const uint2 *tbl = cells + S.table_base;
-    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z > ez) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = cy + dy;
-            if (y < 0 || y > ey) continue;
-            const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-            for (int x = x0; x <= x1; ++x) {
-                const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                uint32_t b = c.x;
-                for (; b + 4 <= c.y; b += 4) {
-                    const float4 p0 = __ldg(&xs[b]), p1 = __ldg(&xs[b + 1]), p2 = __ldg(&xs[b + 2]),
-                                 p3 = __ldg(&xs[b + 3]);
-                    f(b, p0);
-                    f(b + 1, p1);
-                    f(b + 2, p2);
-                    f(b + 3, p3);
-                }
-                for (; b < c.y; ++b) f(b, __ldg(&xs[b]));
-            }
+    for_cell_indices(S, cx, cy, cz, [&](uint32_t k) {
+        const uint2 c = __ldg(&tbl[k]);
+        uint32_t b = c.x;
+        for (; b + 4 <= c.y; b += 4) {
+            const float4 p0 = __ldg(&xs[b]), p1 = __ldg(&xs[b + 1]), p2 = __ldg(&xs[b + 2]), p3 = __ldg(&xs[b + 3]);
+            f(b, p0);
+            f(b + 1, p1);
+            f(b + 2, p2);
+            f(b + 3, p3);
         }
-    }
+        for (; b < c.y; ++b) f(b, __ldg(&xs[b]));
+    });
 }
 
 // Field value, normal and colour sums of one lattice node over its 27 cells.  kUnit:

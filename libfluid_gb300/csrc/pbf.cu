@@ -209,20 +209,9 @@ __device__ __forceinline__ float max_cell_disp(const SceneDev &S, const uint32_t
                                                uint32_t key, uint32_t mbits) {
     const uint32_t m = morton_of(key, mbits);
     const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
-    const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
     const uint32_t *tbl = cellmax + S.table_base;
-    const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
     uint32_t best = 0;  // non-negative floats order like their bit patterns
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z > ez) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = cy + dy;
-            if (y < 0 || y > ey) continue;
-            const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-            for (int x = x0; x <= x1; ++x) best = max(best, __ldg(&tbl[spread10((uint32_t)x) | yz]));
-        }
-    }
+    for_cell_indices(S, cx, cy, cz, [&](uint32_t k) { best = max(best, __ldg(&tbl[k])); });
     return __uint_as_float(best);
 }
 
@@ -265,23 +254,11 @@ struct GlobalSpace {
     template <class F>
     __device__ __forceinline__ void walk(const GatherArgs &A, const SceneDev &S, uint32_t key, F &f) const {
         const uint32_t m = morton_of(key, A.mbits);
-        const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
-        const int ex_ = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
         const uint2 *tbl = A.cells + S.table_base;
-        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex_ ? cx + 1 : ex_;
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int z = cz + dz;
-            if (z < 0 || z > ez) continue;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int y = cy + dy;
-                if (y < 0 || y > ey) continue;
-                const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-                for (int x = x0; x <= x1; ++x) {
-                    const uint2 c = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                    visit(c.x, c.y, f);
-                }
-            }
-        }
+        for_cell_indices(S, (int)compact10(m), (int)compact10(m >> 1), (int)compact10(m >> 2), [&](uint32_t k) {
+            const uint2 c = __ldg(&tbl[k]);
+            visit(c.x, c.y, f);
+        });
     }
     template <class F>
     __device__ __forceinline__ void visit(uint32_t lo, uint32_t hi, F &f) const {
@@ -1202,30 +1179,19 @@ __global__ void k_diffuse(const SceneDev *__restrict__ scenes, uint32_t n, uint3
         const SceneDev &S = scenes[scene_of(key, mbits)];
         const uint32_t m = morton_of(key, mbits);
         const int cx = (int)compact10(m), cy = (int)compact10(m >> 1), cz = (int)compact10(m >> 2);
-        const int ex = (int)S.ext[0], ey = (int)S.ext[1], ez = (int)S.ext[2];
         const uint2 *tbl = cells + S.table_base;
-        const int x0 = cx > 0 ? cx - 1 : 0, x1 = cx < ex ? cx + 1 : ex;
         uint4 s = make_uint4(0, 0, 0, 0);
         uint32_t c = 0;
-        for (int dz = -1; dz <= 1; ++dz) {
-            const int z = cz + dz;
-            if (z < 0 || z > ez) continue;
-            for (int dy = -1; dy <= 1; ++dy) {
-                const int y = cy + dy;
-                if (y < 0 || y > ey) continue;
-                const uint32_t yz = (spread10((uint32_t)y) << 1) | (spread10((uint32_t)z) << 2);
-                for (int x = x0; x <= x1; ++x) {
-                    const uint2 r = __ldg(&tbl[spread10((uint32_t)x) | yz]);
-                    if (r.x >= r.y) continue;
-                    const uint4 g = __ldg(&agg[r.x]);
-                    s.x += g.x;
-                    s.y += g.y;
-                    s.z += g.z;
-                    s.w += g.w;
-                    c += __ldg(&count[r.x]);
-                }
-            }
-        }
+        for_cell_indices(S, cx, cy, cz, [&](uint32_t k) {
+            const uint2 r = __ldg(&tbl[k]);
+            if (r.x >= r.y) return;
+            const uint4 g = __ldg(&agg[r.x]);
+            s.x += g.x;
+            s.y += g.y;
+            s.z += g.z;
+            s.w += g.w;
+            c += __ldg(&count[r.x]);
+        });
         const float t = S.dt / 750.f;
         const float fc = (float)c;
         const uint32_t v = col[a];
