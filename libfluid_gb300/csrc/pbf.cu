@@ -272,37 +272,6 @@ struct GlobalSpace {
         }
         for (; b < hi; ++b) f(b, pos(b));
     }
-    // A range filter over the 27 cells: append(b), in walk order, for the candidates
-    // with test(b, p_b).  Each cell's candidates are tested 32 at a time into a bit
-    // mask and the appends then run over its set bits only, so the append code runs
-    // about as often as a lane has hits rather than once per candidate of the warp.
-    template <class Test, class Append>
-    __device__ __forceinline__ void walk_masked(const GatherArgs &A, const SceneDev &S, uint32_t key, Test &test,
-                                                Append &append) const {
-        const uint32_t m = morton_of(key, A.mbits);
-        const uint2 *tbl = A.cells + S.table_base;
-        for_cell_indices(S, (int)compact10(m), (int)compact10(m >> 1), (int)compact10(m >> 2), [&](uint32_t k) {
-            const uint2 c = __ldg(&tbl[k]);
-            for (uint32_t lo = c.x; lo < c.y; lo += 32) {
-                const uint32_t hi = c.y - lo > 32 ? lo + 32 : c.y;
-                uint32_t mask = 0, b = lo;
-                for (; b + kPrefetch <= hi; b += kPrefetch) {
-                    float4 p[kPrefetch];
-#pragma unroll
-                    for (int j = 0; j < kPrefetch; ++j) p[j] = pos(b + j);
-#pragma unroll
-                    for (int j = 0; j < kPrefetch; ++j)
-                        if (test(b + j, p[j])) mask |= 1u << (b + j - lo);
-                }
-                for (; b < hi; ++b)
-                    if (test(b, pos(b))) mask |= 1u << (b - lo);
-                while (mask) {
-                    append(lo + (uint32_t)(__ffs(mask) - 1));
-                    mask &= mask - 1u;
-                }
-            }
-        });
-    }
 };
 
 // The delta pass's candidates through the lambda pass's copy of p* with each
@@ -401,21 +370,6 @@ __device__ __forceinline__ void for_candidates(const GatherArgs &A, const SceneD
                                                bool list, const Sp &sp, F &&f) {
     if (list) for_row(A.nlist, A.cap, a, A.ncount[a], sp, f);
     else sp.walk(A, S, key, f);
-}
-
-// The candidates with test(b, p_b), appended in walk order: from the Verlet row, or
-// from the 27 cells through the walk's bit masks.
-template <class Sp, class T, class P>
-__device__ __forceinline__ void filter_candidates(const GatherArgs &A, const SceneDev &S, uint32_t a, uint32_t key,
-                                                  bool list, const Sp &sp, T &&test, P &&append) {
-    if (list) {
-        auto f = [&](uint32_t b, const float4 &pb) {
-            if (test(b, pb)) append(b);
-        };
-        for_row(A.nlist, A.cap, a, A.ncount[a], sp, f);
-    } else {
-        sp.walk_masked(A, S, key, test, append);
-    }
 }
 
 // Hit lists.  A lambda pass and the delta pass after it read the same p*, so they
@@ -565,13 +519,10 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, cons
     RowWriter built(A.nlist, A.cap, a);
     // membership only (the passes re-test every entry exactly): a contracted r^2,
     // within ~2e-7 of the sum of squares, against a radius rounded up by 1e-5
-    filter_candidates(
-        A, S, a, key, false, sp,
-        [&](uint32_t, const float4 &pb) {
-            const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-            return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2;
-        },
-        [&](uint32_t b) { built.add(b); });
+    for_candidates(A, S, a, key, false, sp, [&](uint32_t b, const float4 &pb) {
+        const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
+    });
     A.ncount[a] = built.close();
     if (A.over) {  // one atomic per warp, when rows overflowed
         const unsigned m = __activemask();
@@ -676,27 +627,30 @@ __device__ __forceinline__ void lambda_body(const GatherArgs &A, uint32_t a, con
         if (A.hcap == 0 && MODE != kBuild) {
             for_candidates(A, S, a, key, list, sp, body);
         } else {
-            // phase 1: range filter.  (The build pass runs only when the batch keeps no
-            // Verlet lists, A.cap == 0: the list build is k_build_lists.)
+            // phase 1: range filter (and the Verlet list on the build pass)
+            RowWriter built(A.nlist, MODE == kBuild ? A.cap : 0u, a);
             HitWriter hits(A, a);
             const bool near_row =
                 (MODE == kBuild || MODE == kFresh) && A.near && lists_on(A, scene_of(key, A.mbits));
             // membership only (the arithmetic re-tests every entry exactly): a contracted
             // r^2, within ~2e-7 of the sum of squares, against radii rounded up by >= 1e-6
-            const float keep_r2 = near_row ? A.near_r2 : (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
-            filter_candidates(
-                A, S, a, key, list, sp,
-                [&](uint32_t, const float4 &pb) {
-                    const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-                    return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= keep_r2;
-                },
-                [&](uint32_t b) { hits.add(b); });
-            if (MODE == kBuild && A.cap) A.ncount[a] = 0;
+            const float hit_r2 = (PROFILE == kRef ? ph.hh_le : ph.hh) * 1.000001f;
+            for_candidates(A, S, a, key, list, sp, [&](uint32_t b, const float4 &pb) {
+                const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+                const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+                if (MODE == kBuild && r2 <= A.list_r2) built.add(b);
+                if (r2 <= (near_row ? A.near_r2 : hit_r2)) hits.add(b);
+            });
+            if (MODE == kBuild && A.cap) A.ncount[a] = built.close();
             hits.close(A, a);
             if ((MODE == kBuild || MODE == kFresh) && A.over) {  // one atomic per warp, when rows overflowed
                 const unsigned m = __activemask();
+                const unsigned lo = __ballot_sync(m, MODE == kBuild && A.cap && built.count > A.cap);
                 const unsigned ho = __ballot_sync(m, A.hcap && hits.count > A.hcap);
-                if (ho && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
+                if ((lo | ho) && (threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1)) {
+                    if (lo) atomicAdd(&A.over[0], (uint32_t)__popc(lo));
+                    if (ho) atomicAdd(&A.over[1], (uint32_t)__popc(ho));
+                }
             }
             // the first pass sets every mark (none when this step builds no near rows)
             if ((MODE == kBuild || MODE == kFresh) && A.near) A.near[a] = near_row && A.hcap && hits.count <= A.hcap ? 1 : 0;
@@ -1058,7 +1012,6 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
         // phase 1: fluid candidates within h; phase 2: the arithmetic over them
         HitWriter hits(A, a);
         const float hit_r2 = ph.hh * 1.000001f;  // membership only, as in the lambda filter
-        // (a per-candidate filter here: the masked walk measured slower in this kernel)
         for_candidates(A, S, a, key, list, sp, [&](uint32_t b, const float4 &pb) {
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
             const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
