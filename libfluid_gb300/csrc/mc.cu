@@ -8,6 +8,11 @@
 // cube-major order with each cube's triangles in table order -- the order of the
 // reference's CPU marchSingle loop (surface.hpp:185-266), whose edge lerp with its
 // 1e-5 snapping (surface.hpp:47-53) is what the emit kernel evaluates.
+//
+// Layout of the work: the field kernel samples bricks of lattice nodes whose warps
+// share grid cells; the classification runs over 16 consecutive cubes per scan
+// thread; the emit kernel lets each warp gather its cubes that have triangles and
+// write their triangles as whole 128-byte lines.
 #include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
