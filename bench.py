@@ -681,10 +681,14 @@ def run_ours(args):
     algo = ALGO_BYTES[dom] * n
     achieved = algo / (mean_ms / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled(dom, "dam_break_1m")
+    # the summary's figures for the configuration the autotuner chose (near rows with
+    # or without Verlet lists)
+    with_lists = tuned is None or bool(tuned.verlet)
+    suffix = "_with_lists" if with_lists else ""
+    traffic = profiled(dom, "dam_break_1m", "dram_bytes_per_launch" + suffix)
     # the FP32-issue ceiling of the same kernel: its warp instructions per launch
     # (ncu) over the live launch time, against one instruction per scheduler per clock
-    inst = profiled(dom, "dam_break_1m", "warp_inst_per_launch")
+    inst = profiled(dom, "dam_break_1m", "warp_inst_per_launch" + suffix)
     issue = None
     if inst:
         mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
