@@ -440,6 +440,7 @@ def test_near_rows_without_verlet_lists_give_the_same_bits(profile, monkeypatch)
     parts, cfg = scenes.dam_break((24, 16, 24), (2.4, 2.4, 2.4), seed=67)
     parts["type"][::13] = capi.TYPE_OBSTACLE
     solver = SphSolver(params=params)
+    monkeypatch.setenv("FGB_VERLET", "1")
     with_lists = Batch(solver, [(scenes.copy_particles(parts), cfg)])
     with_lists.step(12)
     monkeypatch.setenv("FGB_VERLET", "0")

@@ -35,6 +35,7 @@ def _run(params, parts, cfg, caps, steps):
     # which leaves no rows to grow)
     env = {"FGB_LIST_CAP": str(caps[0]), "FGB_HIT_CAP": str(caps[1])} if caps else {}
     env["FGB_LIST_POLICY"] = "0"
+    env["FGB_VERLET"] = "1"  # the Verlet rows are what grows
     os.environ.update(env)
     try:
         solver = SphSolver(params=params)
@@ -75,12 +76,13 @@ def test_list_policy_changes_no_result(profile):
     parts, cfg = scenes.dam_break((20, 16, 20), (2.0, 1.6, 2.0), seed=93, sphere=(1.0, 0.3, 1.0, 0.3))
     out = {}
     for policy in ("1", "0"):
-        os.environ.update(FGB_LIST_POLICY=policy, FGB_LIST_MIN_USE="95")
+        # with Verlet lists, whose marks tell the steps that built none
+        os.environ.update(FGB_LIST_POLICY=policy, FGB_LIST_MIN_USE="95", FGB_VERLET="1")
         try:
             solver = SphSolver(params=params)
             b = Batch(solver, [(scenes.copy_particles(parts), cfg)])
         finally:
-            del os.environ["FGB_LIST_POLICY"], os.environ["FGB_LIST_MIN_USE"]
+            del os.environ["FGB_LIST_POLICY"], os.environ["FGB_LIST_MIN_USE"], os.environ["FGB_VERLET"]
         off = 0
         for _ in range(40):
             b.step(1)
