@@ -409,6 +409,17 @@ struct RowWriter {
         ++count;
         if ((count & 3u) == 0 && count <= cap) row[(count >> 2) - 1] = q;
     }
+    // add(b) when `hit`, the vector shifted by selects instead of under a branch: the
+    // same entries.  Measured faster in the list build and the vorticity filter (1.1%
+    // off the 64 batched scenes' step), no faster in the lambda filter's walks.
+    __device__ __forceinline__ void add_if(bool hit, uint32_t b) {
+        q.x = hit ? q.y : q.x;
+        q.y = hit ? q.z : q.y;
+        q.z = hit ? q.w : q.z;
+        q.w = hit ? b : q.w;
+        count += hit ? 1u : 0u;
+        if (hit && (count & 3u) == 0 && count <= cap) row[(count >> 2) - 1] = q;
+    }
     // store the last partial vector, its entries moved to the front (the tail entries
     // are stale and never read); returns the row's count, kListOverflow when it did
     // not fit
@@ -521,7 +532,7 @@ __device__ __forceinline__ void build_body(const GatherArgs &A, uint32_t a, cons
     // within ~2e-7 of the sum of squares, against a radius rounded up by 1e-5
     for_candidates(A, S, a, key, false, sp, [&](uint32_t b, const float4 &pb) {
         const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-        if (__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2) built.add(b);
+        built.add_if(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz))) <= A.list_r2, b);
     });
     A.ncount[a] = built.close();
     if (A.over) {  // one atomic per warp, when rows overflowed
@@ -1015,7 +1026,7 @@ __device__ __forceinline__ void vorticity_body(const GatherArgs &A, uint32_t a, 
         for_candidates(A, S, a, key, list, sp, [&](uint32_t b, const float4 &pb) {
             const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
             const float r2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-            if (r2 <= hit_r2 && (!S.obstacles || sp.fluid(b))) hits.add(b);
+            hits.add_if(r2 <= hit_r2 && (!S.obstacles || sp.fluid(b)), b);
         });
         hits.close(A, a);
         if (hits.count <= A.hcap) {
