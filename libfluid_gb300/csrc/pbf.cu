@@ -270,7 +270,15 @@ struct GlobalSpace {
 #pragma unroll
             for (int k = 0; k < kPrefetch; ++k) f(b + k, p[k]);
         }
-        for (; b < hi; ++b) f(b, pos(b));
+        if (b < hi) {  // the last 1-3 candidates, their loads issued together
+            const uint32_t rest = hi - b;
+            const float4 p0 = pos(b);
+            const float4 p1 = rest > 1 ? pos(b + 1) : p0;
+            const float4 p2 = rest > 2 ? pos(b + 2) : p0;
+            f(b, p0);
+            if (rest > 1) f(b + 1, p1);
+            if (rest > 2) f(b + 2, p2);
+        }
     }
 };
 
