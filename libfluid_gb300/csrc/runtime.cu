@@ -564,7 +564,11 @@ struct fgb_batch {
     Dev<uint32_t> queue;
     Dev<uint32_t> list_policy;  // per scene: k_list_policy's state
     Dev<uint32_t> scene_firsts;  // per scene: first triangle of the last batched surface
-    uint32_t list_min_use = 25;  // FGB_LIST_MIN_USE: percent of particles using lists that keeps them
+    // FGB_LIST_MIN_USE: percent of a pass's particles using lists that keeps them on;
+    // by default 25 with Verlet lists and 10 with near rows alone (measured: the near
+    // rows cost little beyond the walk that builds them)
+    uint32_t list_min_use = 0;
+    bool list_min_use_set = false;
     int sm_count = 0;
     float near_frac = 0.05f;  // near-row skin, fraction of h (0: near rows off)
     Dev<uint8_t> near;
@@ -667,7 +671,7 @@ struct fgb_batch {
         s.block = block;
         s.queue = persistent ? queue.p : nullptr;
         s.list_policy = list_policy.p;
-        s.list_min_use = list_min_use;
+        s.list_min_use = list_min_use_set ? list_min_use : (verlet_off ? 10u : 25u);
         s.ppt = persistent ? ppt : 1;
         s.verlet_off = verlet_off;
         s.iterations = iterations;
@@ -1308,7 +1312,10 @@ static int batch_init(fgb_batch *b) {
     FGB_CUDA(b->queue.alloc(slots_of_step(b->iterations)), "batch alloc");
     if (!(getenv("FGB_LIST_POLICY") && strcmp(getenv("FGB_LIST_POLICY"), "0") == 0)) {
         FGB_CUDA(b->list_policy.alloc(kPolicyWords * (uint64_t)b->n_scenes), "batch alloc");
-        if (const char *e = getenv("FGB_LIST_MIN_USE")) b->list_min_use = (uint32_t)std::max(0, std::min(101, atoi(e)));
+        if (const char *e = getenv("FGB_LIST_MIN_USE")) {
+            b->list_min_use = (uint32_t)std::max(0, std::min(101, atoi(e)));
+            b->list_min_use_set = true;
+        }
         std::vector<uint32_t> init(kPolicyWords * (size_t)b->n_scenes, 0u);
         for (uint32_t k = 0; k < b->n_scenes; ++k) init[kPolicyWords * k] = 1u;  // the first step builds lists
         FGB_CUDA(cudaMemcpy(b->list_policy.p, init.data(), init.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
